@@ -1,0 +1,135 @@
+/*
+ * tm_oracle.c -- CPU oracle (TEST INFRASTRUCTURE ONLY; see tm_oracle.h).
+ * Build: gcc -std=c11 -O2 -ffp-contract=off -fno-fast-math -fPIC -shared -fopenmp
+ * (the Makefile beside this file).  -ffp-contract=off matters on aarch64,
+ * where GCC would otherwise fuse a*b+c and change the last bit.
+ */
+#include "tm_oracle.h"
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* Philox4x32-10: J. K. Salmon, M. A. Moraes, R. O. Dror, D. E. Shaw,
+ * "Parallel random numbers: as easy as 1, 2, 3", SC'11.  Ten rounds of
+ * (c0,c1,c2,c3) -> (hi(M1 c2)^c1^k0, lo(M1 c2), hi(M0 c0)^c3^k1, lo(M0 c0))
+ * with the Weyl key schedule between rounds. */
+void tmo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4])
+{
+    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+    uint32_t k0 = key[0], k1 = key[1];
+    for (int r = 0; r < 10; ++r) {
+        if (r > 0) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0;
+        uint32_t n1 = (uint32_t)p1;
+        uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+        uint32_t n3 = (uint32_t)p0;
+        c0 = n0; c1 = n1; c2 = n2; c3 = n3;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+/* ---- double instantiation ---- */
+#define T double
+#define TM_IS_F64 1
+#define FN(name) name##_f64
+#define TC(x) ((double)(x))
+#define FMA fma
+#define SQRT sqrt
+#define FABS fabs
+#define FLOOR floor
+#define RINT rint
+#define TRUNC trunc
+#define LN2_HI 0x1.62e42fee00000p-1
+#define LN2_LO 0x1.a39ef35793c76p-33
+#define INVLN2 0x1.71547652b82fep+0
+#define EXP_XMAX 709.782712893384
+#define EXP_XMIN (-745.1332191019411)
+#include "tm_oracle_prec.inc"
+#undef T
+#undef TM_IS_F64
+#undef FN
+#undef TC
+#undef FMA
+#undef SQRT
+#undef FABS
+#undef FLOOR
+#undef RINT
+#undef TRUNC
+#undef LN2_HI
+#undef LN2_LO
+#undef INVLN2
+#undef EXP_XMAX
+#undef EXP_XMIN
+
+/* ---- float instantiation ---- */
+#define T float
+#define TM_IS_F64 0
+#define FN(name) name##_f32
+#define TC(x) ((float)(x))
+#define FMA fmaf
+#define SQRT sqrtf
+#define FABS fabsf
+#define FLOOR floorf
+#define RINT rintf
+#define TRUNC truncf
+#define LN2_HI 0x1.62ep-1f
+#define LN2_LO 0x1.0bfbe8p-15f
+#define INVLN2 0x1.715476p+0f
+#define EXP_XMAX 88.72283f
+#define EXP_XMIN (-103.972084f)
+#include "tm_oracle_prec.inc"
+
+/* Dornic constants, stochasticSPDP.cpp:952-954 (beta, lambda) with the
+ * beta == 0 limit lambda = 2/(sigma^2 dt) (cf. sde_RFT...DEF.f:48-59).
+ * mean_a1/mean_a2 give the conditional mean of the Dornic kernel,
+ * E[rho*] = e^{beta dt} rho + alpha (e^{beta dt}-1)/beta. */
+void tmo_dornic_consts_compute(double lin, double D, double sigma, double dt, double dx, tmo_dornic_consts* o)
+{
+    double beta = lin - (4.0 * D) / (dx * dx);
+    double e = tmo_exp_f64(beta * dt);
+    double lambda, a2;
+    if (beta == 0.0) {
+        lambda = 2.0 / ((sigma * sigma) * dt);
+        a2 = dt;
+    } else {
+        lambda = (2.0 * beta) / ((sigma * sigma) * (e - 1.0));
+        a2 = (e - 1.0) / beta;
+    }
+    o->beta = beta;
+    o->lambda = lambda;
+    o->expbdt = e;
+    o->pm = lambda * e;
+    o->inv_lambda = 1.0 / lambda;
+    o->mean_a1 = e;
+    o->mean_a2 = a2;
+}
+
+int tmo_dp_batch_run_f32(const tmo_dp_params* p, const int* L, const uint64_t* seed,
+                         float* const* rho, int n_inst, int64_t n_steps, int n_threads)
+{
+    int err = 0;
+#ifdef _OPENMP
+    if (n_threads > 0) omp_set_num_threads(n_threads);
+#pragma omp parallel for schedule(dynamic, 1) reduction(| : err)
+#endif
+    for (int k = 0; k < n_inst; ++k) {
+        int64_t n = (int64_t)L[k] * L[k];
+        float* tmp = (float*)malloc(sizeof(float) * n);
+        if (!tmp) { err |= 1; continue; }
+        float* A = rho[k];
+        float* B = tmp;
+        uint32_t st = 0;
+        for (int64_t s = 0; s < n_steps; ++s) {
+            tmo_dp_step_f32(&p[k], L[k], seed[k], s, A, B, &st);
+            float* t = A; A = B; B = t;
+        }
+        if (A != rho[k]) memcpy(rho[k], A, sizeof(float) * n);
+        free(tmp);
+    }
+    return err ? -1 : 0;
+}

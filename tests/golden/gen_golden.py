@@ -1,0 +1,140 @@
+"""Generate the golden fixtures in this folder from the reference's own code.
+
+Needs the reference checkout and its harness libraries, built by
+`make -C oracle ref` (REF_ROOT defaults to the reference mount of the
+development container).  The fixtures are committed; tests only read them.
+
+    python tests/golden/gen_golden.py
+
+Fixtures
+--------
+ref_pins.npz       deterministic outputs of the reference's stage functions
+                   (noise-off Rietkerk RK4, stochastic-remainder RK4s, the
+                   4th-order noise-off DP RK4, logarithm10_time_bins).
+ref_dp_ensemble.npz  per-replicate trajectories of percolationDornic_2D
+                   (stochasticSPDP.cpp:940), one replicate per call.  The
+                   reference seeds std::mt19937_64 from std::random_device, so
+                   these draws are not reproducible; they are a fixed sample of
+                   the reference's ensemble, compared statistically.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+REF = os.path.join(REPO, "oracle", "_ref")
+dp = C.POINTER(C.c_double)
+
+
+def _p(a):
+    return a.ctypes.data_as(dp)
+
+
+def load():
+    libs = {}
+    for nm in ("dp", "rietkerk", "multisp"):
+        path = os.path.join(REF, f"libref_{nm}.so")
+        if not os.path.exists(path):
+            sys.exit(f"missing {path}: run `make -C oracle ref` first")
+        libs[nm] = C.CDLL(path)
+    d = libs["dp"]
+    d.ref_percolation_dornic.argtypes = [dp, C.c_int, dp] + [C.c_double] * 7 + [C.c_int, C.c_int, dp, C.c_int]
+    d.ref_perc_nodiff.argtypes = [dp, C.c_int, dp] + [C.c_double] * 6 + [C.c_int, dp, C.c_int]
+    d.ref_rk4_first_order.argtypes = [dp, C.c_int] + [C.c_double] * 7
+    d.ref_logarithm10_time_bins.argtypes = [C.c_double, C.c_double, dp, C.c_int]
+    r = libs["rietkerk"]
+    r.ref_rk_det_steps.argtypes = [dp, C.c_int, C.c_int] + [C.c_double] * 14
+    r.ref_rk_stoch_remainder.argtypes = [dp, C.c_int] + [C.c_double] * 12
+    libs["multisp"].ref_ms_rk4_remainder.argtypes = [dp, C.c_int, C.c_double, C.c_double, C.c_double]
+    return libs
+
+
+# Rietkerk parameters of the 256^2 three-field workload (alpha, k2, W0, gmax, k1, c, d, rW, DP, DW, DO, sigma)
+RK = dict(alpha=0.2, k2=5.0, W0=0.2, gmax=0.05, k1=5.0, c=10.0, d=0.25, rW=0.2, DP=0.1, DW=0.1, DO=100.0)
+
+
+def pins(libs, rng):
+    out = {}
+    # 1) noise-off Rietkerk RK4 (f_2D + RK4_Integrate), L=12, 60 steps of dt=1e-3, and a
+    #    larger dt for a stiffer comparison
+    for tag, L, n, dt, R in (("rkdet_a", 12, 60, 1e-3, 0.9), ("rkdet_b", 9, 25, 2e-3, 1.2)):
+        f0 = np.concatenate([rng.uniform(0, 1, L * L), 0.5 + rng.uniform(-0.1, 0.1, L * L),
+                             1.0 + rng.uniform(-0.1, 0.1, L * L)]).astype(np.float64)
+        f = f0.copy()
+        libs["rietkerk"].ref_rk_det_steps(_p(f), L, n, R, RK["c"], RK["gmax"], RK["alpha"], RK["d"], RK["rW"],
+                                          RK["W0"], RK["DP"], RK["DW"], RK["DO"], RK["k1"], RK["k2"], dt, 1.0)
+        out[f"{tag}_in"] = f0.reshape(3, L, L)
+        out[f"{tag}_out"] = f.reshape(3, L, L)
+        out[f"{tag}_meta"] = np.array([L, n, dt, R])
+    # 2) stochastic-remainder RK4 of the Rietkerk step (f_2Dor)
+    L = 10
+    f0 = np.concatenate([rng.uniform(0, 3, L * L), rng.uniform(0.1, 2, L * L), rng.uniform(0.1, 2, L * L)])
+    f = f0.copy()
+    libs["rietkerk"].ref_rk_stoch_remainder(_p(f), L, 0.9, RK["c"], RK["gmax"], RK["alpha"], RK["rW"], RK["W0"],
+                                            RK["DW"], RK["DO"], RK["k1"], RK["k2"], 1e-3, 1.0)
+    out["rkrem_in"] = f0.reshape(3, L, L)
+    out["rkrem_out"] = f.reshape(3, L, L)
+    # 3) MultiSp DP remainder RK4 (f_DP_Dor_1Sp: -b rho^2), b=2, dt=0.1
+    x0 = rng.uniform(0, 3, 100)
+    x = x0.copy()
+    libs["multisp"].ref_ms_rk4_remainder(_p(x), 10, 2.0, 0.1, 1.0)
+    out["msrem_in"], out["msrem_out"] = x0, x
+    # 4) first-order DP remainder RK4 (-b rho^2 - c rho^3), b=-2, c=1 (the first-order model)
+    x0 = rng.uniform(0, 3, 100)
+    x = x0.copy()
+    libs["dp"].ref_rk4_first_order(_p(x), 10, -0.7, -2.0, 1.0, 1.0, 0.0, 0.1, 1.0)
+    out["forem_in"], out["forem_out"] = x0, x
+    # 5) noise-off DP with the 4th-order Laplacian (percNoDiff_2D), L=8, frames after 1, 5, 10 steps
+    L = 8
+    r0 = 0.5 + rng.uniform(-0.2, 0.2, L * L)
+    ts = np.array([0.1, 0.5, 1.0])
+    frames = np.zeros((3, L * L))
+    nf = libs["dp"].ref_perc_nodiff(_p(ts), 3, _p(r0), 1.0, 0.8, 2.0, 1.0, 0.1, 1.0, L, _p(frames), 3)
+    assert nf == 3, nf
+    out["nodiff_in"], out["nodiff_out"] = r0.reshape(L, L), frames.reshape(3, L, L)
+    out["nodiff_meta"] = np.array([L, 0.8, 2.0, 1.0, 0.1, 1.0])  # L a b D dt dx
+    # 6) measurement-time grid
+    cases = [(1e4, 0.1), (1e5, 0.1), (1000.0, 0.01), (100.0, 1.0), (50.0, 0.1), (2.0, 0.1)]
+    for k, (tmax, dt) in enumerate(cases):
+        buf = np.zeros(2000)
+        n = libs["dp"].ref_logarithm10_time_bins(tmax, dt, _p(buf), 2000)
+        out[f"tbins_{k}"] = buf[:n].copy()
+        out[f"tbins_{k}_meta"] = np.array([tmax, dt])
+    return out
+
+
+def ensemble(libs, rng, L, a, tm, n_rep, b=2.0, D=1.0, sigma=1.0, dt=0.1, dx=1.0):
+    tm = np.asarray(tm, np.float64)
+    rho0 = (1.0 + rng.uniform(-0.01, 0.01, L * L)).astype(np.float64)
+    rows = np.zeros((1000, 8))
+    means, act = [], []
+    for _ in range(n_rep):
+        n = libs["dp"].ref_percolation_dornic(_p(tm), len(tm), _p(rho0), tm[-1], a, b, D, sigma, dt, dx, 1, L,
+                                              _p(rows), 1000)
+        means.append(rows[:n, 3].copy())
+        act.append(rows[:n, 6].copy())
+    return dict(t=rows[:n, 2].copy(), mean=np.array(means), active=np.array(act), rho0=rho0.reshape(L, L),
+                meta=np.array([L, a, b, D, sigma, dt, dx]))
+
+
+def main():
+    libs = load()
+    rng = np.random.default_rng(20261203)
+    np.savez_compressed(os.path.join(HERE, "ref_pins.npz"), **pins(libs, rng))
+    ens = {}
+    tm = [1.5, 2.0, 3.0, 5.0, 8.0, 10.0, 20.0, 50.0]
+    for tag, L, a, n in (("crit", 8, 0.72, 1500), ("active", 8, 2.0, 800), ("site", 1, 0.72, 3000)):
+        e = ensemble(libs, rng, L, a, tm, n)
+        for k, v in e.items():
+            ens[f"{tag}_{k}"] = v
+    np.savez_compressed(os.path.join(HERE, "ref_dp_ensemble.npz"), **ens)
+    print("wrote", os.listdir(HERE))
+
+
+if __name__ == "__main__":
+    main()
