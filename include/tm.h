@@ -1,0 +1,195 @@
+/*
+ * tm.h -- C ABI of the GB300 lattice Langevin integrator (libtm.so).
+ *
+ * Drop-in boundary for the per-instance integrators of HAL9K000/Trophic_Maelstorm:
+ *   percolationDornic_2D        simulations/Percolation_FD/stochasticSPDP.cpp:940   (SPDP.h:96)
+ *   dP_Dornic_2D_MultiSp        simulations/Percolation_FD/multiSPDP.cpp:2421
+ *   rietkerk_DorFPE_2D_MultiSp  simulations/Rietkerk_FPE/rietkerk_bjork_FKE.cpp:3697
+ *   rietkerk_Dornic_2D_MultiSp  simulations/Rietkerk_FD/rietkerk_bjork_basic.cpp:3397
+ *   RK4_Wrapper_2D (noise off)  simulations/Rietkerk_FPE/rietkerk_bjork_FKE.cpp:1858
+ *   percNoDiff_2D  (noise off)  simulations/Percolation_FD/stochasticSPDP.cpp:549
+ * The reference calls one of these per parameter value from an OpenMP thread
+ * (stochasticSPDP.cpp:1343-1369) and runs replicates serially inside it.  Here
+ * one call takes a whole batch of instances -- replicates x control values x
+ * lattice sizes, ragged -- and advances them together on one GPU.
+ *
+ * Conventions: plain C types only; host pointers are caller-owned and only
+ * read/written during the call; every function returns TM_OK (0) or a
+ * negative TM_ERR_* code and never exits the process (the reference calls
+ * exit(1|3|4), multiSPDP.cpp:3287-3356).  Per-instance problems found on the
+ * device (NaN/Inf, negative density, sampler iteration cap) are reported as
+ * TM_STATUS_* bits, not as errors.  A context is used by one host thread at a
+ * time; different contexts are independent.
+ *
+ * State layout: a batch keeps all fields of all instances in one packed
+ * buffer of the batch precision (double for TM_FP64, float for TM_FP32).
+ * Instance k starts at element tm_batch_instance_offset(k); inside it the
+ * fields follow each other with stride tm_batch_field_stride(k) elements,
+ * each field an L x L row-major periodic lattice (site i*L + j, the reference's
+ * indexing).  DP has one field (rho); Rietkerk has three in the reference's
+ * order [P, W, O] (rietkerk_bjork_constants_1Sp.h:5-6).
+ */
+#ifndef TM_H
+#define TM_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TM_ABI_VERSION 1
+
+/* return codes */
+#define TM_OK            0
+#define TM_ERR_INVALID  (-1)   /* bad argument                          */
+#define TM_ERR_CUDA     (-2)   /* CUDA runtime error (context unusable)  */
+#define TM_ERR_NOMEM    (-3)   /* device or host allocation failed       */
+#define TM_ERR_STATE    (-4)   /* call not valid in the object's state   */
+
+/* per-instance status bits (OR-ed over all steps since the last reset) */
+#define TM_STATUS_NAN          0x1u  /* NaN or Inf produced               */
+#define TM_STATUS_NEGATIVE     0x2u  /* negative density produced         */
+#define TM_STATUS_SAMPLER_CAP  0x4u  /* a rejection loop hit its cap      */
+
+/* precision of the field state; reductions are FP64 in both */
+#define TM_FP64 0
+#define TM_FP32 1
+
+/* remainder (deterministic part after the Dornic draw) for the DP model */
+#define TM_REM_EULER_EXACT 0   /* rho/(1 + b rho dt)        stochasticSPDP.cpp:1064-1068 */
+#define TM_REM_RK4         1   /* RK4 of -b rho^2 - c rho^3 multiSPDP.cpp:1821-1898      */
+
+/* sampler of the Dornic step */
+#define TM_SAMPLER_EXACT        0  /* Poisson -> Gamma            stochasticSPDP.cpp:1054-1059 */
+#define TM_SAMPLER_REF_GAUSS100 1  /* Gaussian above 100          multiSPDP.cpp:2915-2943      */
+#define TM_SAMPLER_OFF          2  /* conditional mean (noise off)                             */
+
+/* noise-off DP stencils (TM_MODEL_DP_DET) */
+#define TM_STENCIL_5 5   /* 5-point Laplacian                                     */
+#define TM_STENCIL_9 9   /* 4th-order cross (-1,16,-30,16,-1)/12, fP_2D :516-529  */
+
+typedef struct tm_ctx tm_ctx;
+typedef struct tm_batch tm_batch;
+
+/* One lattice instance of a batch. */
+typedef struct tm_instance {
+    int32_t  L;        /* lattice side, >= 1                                         */
+    int32_t  reserved;
+    uint64_t seed;     /* Philox key of this instance's random stream               */
+    double   a;        /* DP: linear coefficient a at step 0; Rietkerk: rainfall R  */
+    double   a_step;   /* DP: a(s) = a + a_step * s (0 = fixed a); Rietkerk: unused */
+} tm_instance;
+
+/* DP Langevin model  d rho = (a rho - b rho^2 - c rho^3 + D Lap rho) dt + sigma sqrt(rho) dW
+ * (stochasticSPDP.cpp:940-1068, multiSPDP.cpp:2421-3262).  a is per instance. */
+typedef struct tm_dp_model {
+    double b, c, D, sigma, dt, dx;
+    double clamp_lo, clamp_eps;  /* after each step clamp_lo <= rho < clamp_eps -> 0;
+                                    clamp_eps = 0 disables (classic); multiSPDP uses
+                                    [-1e-80, 1e-12) (:3256-3259)                     */
+    int32_t remainder;           /* TM_REM_*                                        */
+    int32_t sampler;             /* TM_SAMPLER_*                                    */
+    int32_t deterministic;       /* 1: noise-off a rho - b rho^2 - c rho^3 + D Lap rho
+                                    by RK4/Euler on the lattice, no Dornic split
+                                    (percNoDiff_2D); uses stencil and integrator    */
+    int32_t stencil;             /* TM_STENCIL_5 / TM_STENCIL_9 (deterministic only) */
+    int32_t integrator;          /* 0 Euler, 1 RK4 (deterministic only)             */
+    int32_t reserved;
+} tm_dp_model;
+
+/* Rietkerk three-field vegetation model (rietkerk_bjork_FKE.cpp:1760-1785, 2363-2390):
+ *   dO = R - alpha O (P + k2 W0)/(P + k2) + D_O Lap O
+ *   dW = alpha O (P + k2 W0)/(P + k2) - gmax W P/(W + k1) - rW W + D_W Lap W
+ *   dP = c gmax W P/(W + k1) - d P + D_P Lap P + sigma sqrt(P) dW
+ * R is per instance (tm_instance.a).  With deterministic = 0 the -d P + D_P Lap P
+ * + noise part is the Dornic draw and the rest is one RK4 step; with
+ * deterministic = 1 the whole right-hand side is one RK4 step (RK4_Wrapper_2D). */
+typedef struct tm_rietkerk_model {
+    double alpha, k2, W0, gmax, k1, c, d, rW;
+    double DP, DW, DO, sigma, dt, dx;
+    double clamp_lo, clamp_eps;  /* reference: 0 <= x < 1e-10 -> 0 (:4460, basic.h:119) */
+    int32_t sampler;             /* TM_SAMPLER_*, reference: TM_SAMPLER_REF_GAUSS100 */
+    int32_t deterministic;
+} tm_rietkerk_model;
+
+/* -------------------------------------------------------------------- */
+int         tm_abi_version(void);
+const char* tm_error_string(int code);
+
+/* Context on one CUDA device with its own stream. */
+int   tm_create(tm_ctx** out, int device);
+int   tm_destroy(tm_ctx* ctx);
+void* tm_stream(tm_ctx* ctx);            /* the cudaStream_t the context launches on */
+int   tm_sync(tm_ctx* ctx);
+
+/* -- batches: device-resident state advanced step by step ------------------ */
+/* Replaces the replicate/parameter loops around percolationDornic_2D
+ * (stochasticSPDP.cpp:1343-1384) and rietkerk_DorFPE_2D_MultiSp (:4778-4802). */
+int tm_batch_create_dp(tm_ctx* ctx, const tm_dp_model* model, const tm_instance* inst,
+                       int n_inst, int precision, tm_batch** out);
+int tm_batch_create_rietkerk(tm_ctx* ctx, const tm_rietkerk_model* model, const tm_instance* inst,
+                             int n_inst, int precision, tm_batch** out);
+int tm_batch_destroy(tm_batch* b);
+
+int64_t tm_batch_total_elems(const tm_batch* b);          /* packed state size (elements) */
+int64_t tm_batch_instance_offset(const tm_batch* b, int k);
+int64_t tm_batch_field_stride(const tm_batch* b, int k);
+int     tm_batch_num_fields(const tm_batch* b);            /* 1 (DP) or 3 (Rietkerk)       */
+int     tm_batch_obs_width(const tm_batch* b);             /* doubles per measurement      */
+int64_t tm_batch_step(const tm_batch* b);                  /* steps taken so far           */
+
+/* State transfer; host_fields/dev_fields hold tm_batch_total_elems() elements of
+ * the batch precision in the packed layout.  Upload resets the step counter to
+ * `step` (the Philox counter of the next step) and revives extinct instances. */
+int tm_batch_upload(tm_batch* b, const void* host_fields, int64_t step);
+int tm_batch_download(tm_batch* b, void* host_fields);
+int tm_batch_upload_device(tm_batch* b, const void* dev_fields, int64_t step);
+int tm_batch_download_device(tm_batch* b, void* dev_fields);
+/* Copy one instance's fields (nf * L * L elements, fields contiguous) to host:
+ * the frame interface of save_frame (multiSPDP.cpp:1596-1643). */
+int tm_batch_snapshot(tm_batch* b, int k, void* host_out);
+
+/* Advance n_steps steps.  Before the step with absolute index s (i.e. on the
+ * state after s steps) every s listed in meas_steps (ascending, each in
+ * [tm_batch_step, tm_batch_step + n_steps]) is measured into
+ * obs[(j * n_inst + k) * obs_width + f]:
+ *   DP:        f0 = spatial mean of rho, f1 = number of sites with rho > 0
+ *   Rietkerk:  f0..f2 = spatial means of P, W, O, f3 = sites with P > 0
+ * (mean_of_vector / occupied_sites_of_vector, stochasticSPDP.cpp:123-154).  A DP
+ * instance measured with no active site is extinct: it stays zero and its
+ * later measurements are 0 (the early exit of stochasticSPDP.cpp:1021-1022).
+ * status (optional, n_inst entries) receives the OR of TM_STATUS_* bits since
+ * creation or the last upload.  obs may be NULL when n_meas == 0.
+ * The call returns after the work is queued and complete (it synchronises). */
+int tm_batch_advance(tm_batch* b, int64_t n_steps, const int64_t* meas_steps, int n_meas,
+                     double* obs, uint32_t* status);
+/* Same, without synchronising and without measurements: queues n_steps steps on
+ * the context stream (CUDA graphs of the step sequence); for timing loops. */
+int tm_batch_enqueue_steps(tm_batch* b, int64_t n_steps);
+
+/* Launch shape of the step kernels: rows per warp task (DP/Dornic) and CTAs
+ * per SM of the persistent grid.  0 keeps the current value.  tm_batch_autotune
+ * times the candidates on the batch itself (state is saved and restored). */
+int tm_batch_set_launch(tm_batch* b, int rows_per_task, int ctas_per_sm);
+int tm_batch_get_launch(const tm_batch* b, int* rows_per_task, int* ctas_per_sm);
+int tm_batch_autotune(tm_batch* b, int steps_per_trial);
+
+/* -- one-shot calls: host buffers in, host results out -------------------- */
+/* The whole percolationDornic_2D-style job for a batch: upload init_fields,
+ * advance n_steps with measurements, return obs/status and (optionally) the
+ * final fields.  Host<->device copies are part of the call. */
+int tm_run_dp(tm_ctx* ctx, const tm_dp_model* model, const tm_instance* inst, int n_inst, int precision,
+              const void* init_fields, int64_t n_steps, const int64_t* meas_steps, int n_meas,
+              double* obs, uint32_t* status, void* final_fields);
+int tm_run_rietkerk(tm_ctx* ctx, const tm_rietkerk_model* model, const tm_instance* inst, int n_inst,
+                    int precision, const void* init_fields, int64_t n_steps, const int64_t* meas_steps,
+                    int n_meas, double* obs, uint32_t* status, void* final_fields);
+
+/* Packed-layout geometry without a batch (for callers that pack host buffers
+ * before creating one): offsets[k] and the total, for nf fields per instance. */
+int64_t tm_layout(const tm_instance* inst, int n_inst, int nf, int64_t* offsets, int64_t* field_strides);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,291 @@
+"""GPU kernels (through the C ABI) against the CPU oracle.
+
+The kernels and the oracle implement one operation-by-operation specification
+of the Dornic step (same Philox stream, same own log/exp, same evaluation
+order), so fields must agree bit for bit in FP64 and in FP32; spatial means are
+FP64 sums in a different order and must agree to 1e-12 relative; active-site
+counts exactly.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+MEAN_RTOL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def tmg():
+    from trophic_maelstorm_gb300 import build
+    build.build()
+    import trophic_maelstorm_gb300 as m
+    return m
+
+
+@pytest.fixture(scope="module")
+def ctx(tmg):
+    return tmg.Context(0)
+
+
+def _init_fields(Ls, seed, zeros=True):
+    rng = np.random.default_rng(seed)
+    out = []
+    for L in Ls:
+        f = 1.0 + rng.uniform(-0.01, 0.01, (L, L))
+        if zeros and L >= 4:
+            f[: L // 2, : L // 3] = 0.0      # an absorbing patch
+            f[L - 1, L - 1] = 1e-30          # a nearly empty site
+        out.append(f)
+    return out
+
+
+def _oracle_dp_params(oracle, model, a, a_step):
+    return oracle.DPParams(a, a_step, model.b, model.c, model.D, model.sigma, model.dt, model.dx, model.clamp_lo,
+                           model.clamp_eps, model.remainder, model.sampler)
+
+
+def _compare_dp(tmg, oracle, ctx, model, Ls, a, a_step, n_steps, meas, precision, seed0=11, init_seed=0,
+                zeros=True):
+    dtype = np.float64 if precision == tmg.TM_FP64 else np.float32
+    seeds = [seed0 + 7 * k for k in range(len(Ls))]
+    inst = tmg.instances(Ls, seeds, a, a_step)
+    init = [f.astype(dtype) for f in _init_fields(Ls, init_seed, zeros)]
+    b = tmg.Batch(ctx, model, inst, precision)
+    b.upload(init)
+    obs, st = b.advance(n_steps, meas)
+    fin = b.download()
+    aa = np.broadcast_to(np.asarray(a, float), (len(Ls),))
+    asx = np.broadcast_to(np.asarray(a_step, float), (len(Ls),))
+    for k, L in enumerate(Ls):
+        p = _oracle_dp_params(oracle, model, aa[k], asx[k])
+        m, act, ofin, ost = oracle.dp_run(p, init[k], seeds[k], n_steps, meas)
+        assert np.array_equal(fin[k], ofin), (k, L, np.max(np.abs(fin[k] - ofin)))
+        np.testing.assert_allclose(obs[:, k, 0], m, rtol=MEAN_RTOL, atol=0)
+        assert np.array_equal(obs[:, k, 1], act), (k, L)
+        assert st[k] == ost, (k, st[k], ost)
+    b.close()
+    return obs, st, fin
+
+
+LS = [1, 3, 8, 33, 64, 100]
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32"])
+@pytest.mark.parametrize("sampler", [0, 1, 2], ids=["exact", "gauss100", "off"])
+@pytest.mark.parametrize("remainder", [0, 1], ids=["euler", "rk4"])
+def test_dp_step_matches_oracle(tmg, oracle, ctx, precision, sampler, remainder):
+    model = tmg.dp_model(b=2.0, D=1.0, sigma=1.0, dt=0.1, remainder=remainder, sampler=sampler)
+    _compare_dp(tmg, oracle, ctx, model, LS, 0.72, 0.0, 6, [0, 1, 3, 6], precision)
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32"])
+def test_dp_graph_chunks_and_ramp(tmg, oracle, ctx, precision):
+    # 100 steps: graph replays of 32 steps between measurements, direct steps around them;
+    # a ramped 0.72 -> 0.70 as in the 128^2 workload
+    model = tmg.dp_model()
+    n = 100
+    _compare_dp(tmg, oracle, ctx, model, [16, 40, 128], 0.72, (0.70 - 0.72) / n, n, [0, 5, 37, 38, 100],
+                precision)
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32"])
+def test_dp_multisp_clamp_and_first_order(tmg, oracle, ctx, precision):
+    # multiSPDP semantics: RK4 remainder, Gaussian above 100, clamp [-1e-80, 1e-12) -> 0
+    m1 = tmg.dp_model(b=2.0, remainder=1, sampler=1, clamp_lo=-1e-80, clamp_eps=1e-12)
+    _compare_dp(tmg, oracle, ctx, m1, [8, 50], 0.72, 0.0, 20, [0, 10, 20], precision)
+    # first-order model: a < 0, b < 0, cubic c > 0 (stochasticSPDP.cpp:1766-1805)
+    m2 = tmg.dp_model(b=-2.0, c=1.0, remainder=1)
+    _compare_dp(tmg, oracle, ctx, m2, [8, 50], -0.7, 0.0, 20, [0, 10, 20], precision)
+
+
+def test_dp_extinction(tmg, oracle, ctx):
+    model = tmg.dp_model(b=2.0)
+    Ls = [8, 12]
+    inst = tmg.instances(Ls, [1, 2], -5.0)  # strongly absorbing
+    init = [np.zeros((8, 8)), np.zeros((12, 12))]
+    init[0][3, 3] = 1e-3
+    init[1][5, 5] = 1.0
+    b = tmg.Batch(ctx, model, inst, tmg.TM_FP64)
+    b.upload(init)
+    meas = [0, 1, 2, 5, 10, 40, 60]
+    obs, st = b.advance(60, meas)
+    fin = b.download()
+    for k in range(2):
+        p = oracle.DPParams(-5.0, 0.0, 2.0, 0.0, 1.0, 1.0, 0.1, 1.0, 0.0, 0.0, 0, 0)
+        m, act, ofin, _ = oracle.dp_run(p, init[k], k + 1, 60, meas)
+        np.testing.assert_allclose(obs[:, k, 0], m, rtol=MEAN_RTOL, atol=0)
+        assert np.array_equal(obs[:, k, 1], act)
+        assert np.array_equal(fin[k], ofin)
+    assert obs[-1, :, 1].sum() == 0  # both extinct by t = 6
+    b.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32"])
+def test_launch_shape_and_path_invariance(tmg, ctx, precision):
+    """Rows per task, CTAs per SM and graph vs direct launches change nothing."""
+    model = tmg.dp_model()
+    Ls = [64, 128, 96]
+    inst = tmg.instances(Ls, [5, 6, 7], 0.72)
+    dtype = np.float64 if precision == 0 else np.float32
+    init = [f.astype(dtype) for f in _init_fields(Ls, 3)]
+    res = []
+    for rows, ctas, chunks in ((32, 4, [70]), (8, 2, [70]), (64, 8, [70]), (16, 1, [1] * 70)):
+        b = tmg.Batch(ctx, model, inst, precision)
+        b.set_launch(rows, ctas)
+        b.upload(init)
+        for c in chunks:
+            b.advance(c)
+        res.append(b.download_packed())
+        b.close()
+    for r in res[1:]:
+        assert np.array_equal(r, res[0])
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32"])
+@pytest.mark.parametrize("sampler", [1, 0], ids=["gauss100", "exact"])
+def test_rietkerk_matches_oracle(tmg, oracle, ctx, precision, sampler):
+    model = tmg.rietkerk_model(sampler=sampler)
+    Ls = [5, 16, 37]
+    R = [0.6, 0.9, 1.2]
+    dtype = np.float64 if precision == 0 else np.float32
+    rng = np.random.default_rng(1)
+    init = [np.stack([rng.uniform(0, 1, (L, L)), np.full((L, L), 0.5), np.full((L, L), 1.0)]).astype(dtype)
+            for L in Ls]
+    inst = tmg.instances(Ls, [3, 4, 5], R)
+    b = tmg.Batch(ctx, model, inst, precision)
+    b.upload(init)
+    meas = [0, 7, 15]
+    obs, st = b.advance(15, meas)
+    fin = b.download()
+    for k, L in enumerate(Ls):
+        p = oracle.rk_params(R=R[k], sampler=sampler)
+        m, act, ofin, ost = oracle.rk_run(p, init[k], [3, 4, 5][k], 15, meas)
+        assert np.array_equal(fin[k], ofin), (k, np.max(np.abs(fin[k] - ofin)))
+        np.testing.assert_allclose(obs[:, k, :3], m, rtol=MEAN_RTOL, atol=0)
+        assert np.array_equal(obs[:, k, 3], act)
+        assert st[k] == ost
+    b.close()
+
+
+def test_rietkerk_noise_off_matches_reference(tmg, ctx, golden):
+    """Noise-off Rietkerk RK4 (f_2D / RK4_Integrate) on the GPU against the reference's
+    own output, to 1e-10 relative (the spec noise-off bar)."""
+    g = golden["pins"]
+    for tag in ("rkdet_a", "rkdet_b"):
+        L, n, dt, R = g[f"{tag}_meta"]
+        L, n = int(L), int(n)
+        model = tmg.rietkerk_model(dt=dt, deterministic=1)
+        b = tmg.Batch(ctx, model, tmg.instances([L], [0], R), tmg.TM_FP64)
+        b.upload([g[f"{tag}_in"]])
+        b.advance(n)
+        out = b.download()[0]
+        np.testing.assert_allclose(out, g[f"{tag}_out"], rtol=1e-10, atol=0)
+        b.close()
+
+
+@pytest.mark.parametrize("stencil", [5, 9])
+@pytest.mark.parametrize("integrator", [0, 1])
+def test_dp_noise_off_lattice_matches_oracle(tmg, oracle, ctx, stencil, integrator):
+    model = tmg.dp_model(b=2.0, c=0.5, D=1.0, dt=0.05, deterministic=1, stencil=stencil, integrator=integrator)
+    Ls = [7, 32]
+    init = _init_fields(Ls, 4, zeros=False)
+    b = tmg.Batch(ctx, model, tmg.instances(Ls, [0, 0], 0.8), tmg.TM_FP64)
+    b.upload(init)
+    b.advance(12)
+    fin = b.download()
+    for k in range(2):
+        r = init[k]
+        for _ in range(12):
+            r = oracle.dp_det_step(r, 0.8, 2.0, 0.5, 1.0, 0.05, 1.0, stencil=stencil, integrator=integrator)
+        assert np.array_equal(fin[k], r)
+    b.close()
+
+
+def test_dp_noise_off_4th_order_matches_reference(tmg, ctx, golden):
+    g = golden["pins"]
+    L, a, b_, D, dt, dx = g["nodiff_meta"]
+    model = tmg.dp_model(b=b_, D=D, dt=dt, dx=dx, deterministic=1, stencil=9, integrator=1)
+    b = tmg.Batch(ctx, model, tmg.instances([int(L)], [0], a), tmg.TM_FP64)
+    b.upload([g["nodiff_in"]])
+    frames = []
+    for _ in range(10):
+        b.advance(1)
+        frames.append(b.download()[0])
+    got = np.array([frames[0], frames[4], frames[9]])
+    np.testing.assert_allclose(got, g["nodiff_out"], rtol=1e-10, atol=0)
+    b.close()
+
+
+def test_full_size_step_matches_oracle(tmg, oracle, ctx):
+    """Two steps of a 1024^2 FP32 lattice, bit for bit."""
+    model = tmg.dp_model()
+    L = 1024
+    rng = np.random.default_rng(2)
+    init = (1.0 + rng.uniform(-0.01, 0.01, (L, L))).astype(np.float32)
+    b = tmg.Batch(ctx, model, tmg.instances([L], [99], 0.72), tmg.TM_FP32)
+    b.upload([init])
+    obs, st = b.advance(2, [0, 2])
+    fin = b.download()[0]
+    p = oracle.dp_params(a=0.72)
+    m, act, ofin, ost = oracle.dp_run(p, init, 99, 2, [0, 2])
+    assert np.array_equal(fin, ofin)
+    np.testing.assert_allclose(obs[:, 0, 0], m, rtol=MEAN_RTOL)
+    assert np.array_equal(obs[:, 0, 1], act)
+    b.close()
+
+
+def test_one_shot_call_equals_batch(tmg, ctx):
+    model = tmg.dp_model()
+    Ls = [24, 64]
+    inst = tmg.instances(Ls, [3, 4], 0.72)
+    init = tmg.pack(_init_fields(Ls, 9), inst, 1, np.float32)
+    obs1, st1, fin1 = tmg.run_dp(ctx, model, inst, init, 40, [0, 20, 40], tmg.TM_FP32)
+    b = tmg.Batch(ctx, model, inst, tmg.TM_FP32)
+    b.upload(init)
+    obs2, st2 = b.advance(40, [0, 20, 40])
+    assert np.array_equal(obs1, obs2) and np.array_equal(fin1, b.download_packed())
+    b.close()
+
+
+def test_reproducible_per_seed(tmg, ctx):
+    model = tmg.dp_model()
+    inst = tmg.instances([256, 512], [1, 2], 0.72)
+    init = tmg.pack(_init_fields([256, 512], 1), inst, 1, np.float32)
+    outs = []
+    for _ in range(2):
+        obs, st, fin = tmg.run_dp(ctx, model, inst, init, 50, [50], tmg.TM_FP32)
+        outs.append((obs, fin))
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+    inst2 = tmg.instances([256, 512], [3, 2], 0.72)
+    obs, st, fin = tmg.run_dp(ctx, model, inst2, init, 50, [50], tmg.TM_FP32)
+    assert not np.array_equal(fin[:256 * 256], outs[0][1][:256 * 256])
+    assert np.array_equal(fin[256 * 256:], outs[0][1][256 * 256:])
+
+
+def test_gpu_ensemble_matches_reference(tmg, ctx, golden):
+    """percolation_dornic_2d on the GPU (1500 replicates in one batch) against the
+    reference's ensemble: rho(t) within 3.5 combined SE and KS p > 0.01/n_t."""
+    from scipy import stats
+    ens = golden["ens"]
+    L, a, b, D, sig, dt, dx = ens["crit_meta"]
+    t = ens["crit_t"]
+    steps = np.rint(t / dt).astype(np.int64)
+    r = 1500
+    inst = tmg.instances([int(L)] * r, range(5000, 5000 + r), a)
+    model = tmg.dp_model(b=b, D=D, sigma=sig, dt=dt, dx=dx)
+    init = tmg.pack([ens["crit_rho0"]] * r, inst, 1, np.float64)
+    obs, st, _ = tmg.run_dp(ctx, model, inst, init, int(steps[-1]), steps, tmg.TM_FP64)
+    M = obs[:, :, 0].T
+    R = ens["crit_mean"]
+    for j in range(1, len(t)):
+        se = np.sqrt(M[:, j].var() / r + R[:, j].var() / len(R))
+        assert abs(M[:, j].mean() - R[:, j].mean()) < 3.5 * se
+        assert stats.ks_2samp(M[:, j], R[:, j]).pvalue > 0.01 / len(t)
+
+
+def test_reference_rows_shape(tmg, ctx):
+    rows, st = tmg.percolation_dornic_2d([1.5, 2.0, 5.0], np.ones(64), 5.0, 0.72, 2.0, 1.0, 1.0, 0.1, 1.0, 8, 8,
+                                         seed=3, ctx=ctx)
+    assert rows.shape == (11 + 3, 8)
+    assert np.allclose(rows[:, 0], 0.72) and np.allclose(rows[:, 1], 8)
+    assert rows[0, 3] == pytest.approx(1.0) and rows[0, 5] == 8

@@ -1,0 +1,75 @@
+"""Host-side logic and the C ABI surface (no GPU needed)."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def tmlib():
+    from trophic_maelstorm_gb300 import build, _lib
+    build.build()
+    return _lib
+
+
+def test_library_exports_every_declared_symbol(tmlib):
+    hdr = open(os.path.join(REPO, "include", "tm.h")).read()
+    hdr = re.sub(r"/\*.*?\*/", "", hdr, flags=re.S)
+    declared = set(re.findall(r"\b(tm_[a-z0-9_]+)\s*\(", hdr))
+    assert declared, "no declarations parsed"
+    lib = C.CDLL(tmlib.LIB_PATH)
+    missing = [s for s in sorted(declared) if not hasattr(lib, s)]
+    assert not missing, missing
+    assert declared == set(tmlib.EXPORTS)
+    assert tmlib.lib().tm_abi_version() == 1
+    assert tmlib.lib().tm_error_string(-1) == b"invalid argument"
+
+
+def test_layout_is_aligned_and_packs_round_trip(tmlib):
+    import trophic_maelstorm_gb300 as tmg
+    inst = tmg.instances([1, 3, 33, 64, 100], range(5), 0.7)
+    for nf in (1, 3):
+        total, off, fs = tmg.layout(inst, nf)
+        assert all(o % 32 == 0 for o in off) and all(f % 32 == 0 for f in fs)
+        assert total == off[-1] + nf * fs[-1]
+        rng = np.random.default_rng(nf)
+        fields = [rng.random((nf, i.L, i.L)) if nf > 1 else rng.random((i.L, i.L)) for i in inst]
+        back = tmg.unpack(tmg.pack(fields, inst, nf, np.float64), inst, nf)
+        for a, b in zip(fields, back):
+            assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("k", range(6))
+def test_time_bins_match_reference(golden, k):
+    import trophic_maelstorm_gb300 as tmg
+    g = golden["pins"]
+    tmax, dt = g[f"tbins_{k}_meta"]
+    assert np.array_equal(np.array(tmg.logarithm10_time_bins(tmax, dt)), g[f"tbins_{k}"])
+
+
+def test_reference_step_grid():
+    import trophic_maelstorm_gb300 as tmg
+    steps, times, n_early = tmg.reference_step_grid([1.5, 2.0, 10.0], 0.1)
+    assert n_early == 11 and steps[:11] == list(range(11)) and steps[11:] == [15, 20, 100]
+
+
+def test_replicate_rows_statistics():
+    import trophic_maelstorm_gb300 as tmg
+    mean = np.array([[1.0, 0.5, 0.2], [1.0, 0.7, 0.0], [1.0, 0.3, 0.4]])
+    act = np.array([[4, 2, 1], [4, 3, 0], [4, 1, 2]], float)
+    rows = tmg.replicate_rows(0.7, 2, [0.0, 0.1, 2.0], 2, mean, act)
+    assert rows.shape == (3, 8)
+    assert rows[2, 5] == 2 and rows[2, 3] == pytest.approx(0.3) and rows[2, 4] == pytest.approx(0.02)
+    assert rows[1, 4] == pytest.approx(np.var([0.5, 0.7, 0.3], ddof=1))
+    assert rows[0, 7] == 3 and rows[2, 7] == 2
+
+
+def test_invalid_arguments_are_rejected_without_gpu(tmlib):
+    L = tmlib.lib()
+    assert L.tm_create(None, 0) == tmlib.TM_ERR_INVALID
+    assert L.tm_destroy(None) == tmlib.TM_ERR_INVALID
+    assert L.tm_batch_step(None) == -1

@@ -1,0 +1,93 @@
+"""The oracle against the reference's own code (golden fixtures made by
+tests/golden/gen_golden.py from the compiled reference sources)."""
+import numpy as np
+import pytest
+from scipy import stats
+
+
+def test_philox_known_answers(oracle):
+    # Random123 known-answer vectors for Philox4x32-10
+    assert [hex(v) for v in oracle.philox([0, 0, 0, 0], [0, 0])] == \
+        ["0x6627e8d5", "0xe169c58d", "0xbc57ac4c", "0x9b00dbd8"]
+    assert [hex(v) for v in oracle.philox([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2)] == \
+        ["0x408f276d", "0x41c83b0e", "0xa20bc7c6", "0x6d5451fd"]
+    assert [hex(v) for v in oracle.philox([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344],
+                                          [0xA4093822, 0x299F31D0])] == \
+        ["0xd16cfe09", "0x94fdcceb", "0x5001e420", "0x24126ea1"]
+
+
+@pytest.mark.parametrize("tag", ["rkdet_a", "rkdet_b"])
+def test_rietkerk_noise_off_rk4_matches_reference(oracle, golden, tag):
+    g = golden["pins"]
+    L, n, dt, R = g[f"{tag}_meta"]
+    p = oracle.rk_params(R=R, dt=dt)
+    f = g[f"{tag}_in"].copy()
+    for _ in range(int(n)):
+        f = oracle.rk_det_step(p, f)
+    ref = g[f"{tag}_out"]
+    np.testing.assert_allclose(f, ref, rtol=1e-10, atol=0)
+    assert np.array_equal(f, ref)  # same operation order: identical bits
+
+
+def test_rietkerk_stochastic_remainder_matches_reference(oracle, golden):
+    g = golden["pins"]
+    f = oracle.rk_remainder(oracle.rk_params(R=0.9, dt=1e-3), g["rkrem_in"])
+    np.testing.assert_allclose(f, g["rkrem_out"], rtol=1e-10, atol=0)
+    assert np.array_equal(f, g["rkrem_out"])
+
+
+def test_multisp_rk4_remainder_matches_reference(oracle, golden):
+    g = golden["pins"]
+    x = oracle.dp_remainder(oracle.dp_params(b=2.0, dt=0.1, remainder=oracle.REM_RK4), g["msrem_in"])
+    assert np.array_equal(x, g["msrem_out"])
+
+
+def test_first_order_rk4_remainder_matches_reference(oracle, golden):
+    g = golden["pins"]
+    x = oracle.dp_remainder(oracle.dp_params(b=-2.0, c=1.0, dt=0.1, remainder=oracle.REM_RK4), g["forem_in"])
+    assert np.array_equal(x, g["forem_out"])
+
+
+def test_dp_noise_off_4th_order_matches_reference(oracle, golden):
+    g = golden["pins"]
+    L, a, b, D, dt, dx = g["nodiff_meta"]
+    r = g["nodiff_in"].copy()
+    frames = []
+    for _ in range(10):
+        r = oracle.dp_det_step(r, a, b, 0.0, D, dt, dx, stencil=9, integrator=1)
+        frames.append(r)
+    got = np.array([frames[0], frames[4], frames[9]])
+    np.testing.assert_allclose(got, g["nodiff_out"], rtol=1e-10, atol=0)
+
+
+def _oracle_ensemble(oracle, ens, tag, n_rep, seed0=1000):
+    L, a, b, D, sig, dt, dx = ens[f"{tag}_meta"]
+    steps = np.rint(ens[f"{tag}_t"] / dt).astype(np.int64)
+    p = oracle.dp_params(a=a, b=b, D=D, sigma=sig, dt=dt, dx=dx)
+    M, A = [], []
+    for k in range(n_rep):
+        m, act, _, st = oracle.dp_run(p, ens[f"{tag}_rho0"], seed0 + k, int(steps[-1]), steps)
+        assert st == 0
+        M.append(m); A.append(act)
+    return np.array(M), np.array(A)
+
+
+@pytest.mark.parametrize("tag,n_rep", [("crit", 1500), ("active", 400), ("site", 3000)])
+def test_dp_ensemble_matches_reference(oracle, golden, tag, n_rep):
+    """rho(t), survival and the distribution of rho(t) over replicates agree with the
+    reference's percolationDornic_2D ensemble: means within 3 combined standard errors,
+    two-sample KS p > 0.01 at every time (Bonferroni over the time points)."""
+    ens = golden["ens"]
+    M, A = _oracle_ensemble(oracle, ens, tag, n_rep)
+    R, RA = ens[f"{tag}_mean"], ens[f"{tag}_active"]
+    n_t = R.shape[1]
+    for j in range(1, n_t):
+        se = np.sqrt(M[:, j].var() / len(M) + R[:, j].var() / len(R))
+        if se > 0:
+            assert abs(M[:, j].mean() - R[:, j].mean()) < 3.5 * se, (tag, j)
+        ps, pr = (A[:, j] > 0).mean(), (RA[:, j] > 0).mean()
+        se_s = np.sqrt(ps * (1 - ps) / len(A) + pr * (1 - pr) / len(RA))
+        if se_s > 0:
+            assert abs(ps - pr) < 3.5 * se_s, (tag, j)
+        if M[:, j].std() > 0 and R[:, j].std() > 0:
+            assert stats.ks_2samp(M[:, j], R[:, j]).pvalue > 0.01 / n_t, (tag, j)

@@ -1,0 +1,84 @@
+"""The oracle's samplers against scipy's distributions and the published
+properties of the Dornic transition kernel."""
+import numpy as np
+import pytest
+from scipy import stats
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("m", [1e-3, 0.5, 3.7, 9.99, 10.0, 17.0, 250.0, 1e4])
+def test_poisson_chi2(oracle, dtype, m):
+    N = 100000
+    x, st = oracle.sample("poisson", N, seed=7, m=m, dtype=dtype)
+    assert st == 0
+    sd = np.sqrt(m)
+    lo, hi = max(0, int(m - 6 * sd)), int(m + 6 * sd) + 2
+    edges = np.unique(np.linspace(lo, hi, min(40, hi - lo + 1)).astype(int))
+    obs, _ = np.histogram(x, bins=np.concatenate([[-np.inf], edges, [np.inf]]))
+    cdf = np.concatenate([[0.0], stats.poisson.cdf(edges - 1, m), [1.0]])
+    exp = np.diff(cdf) * N
+    keep = exp > 10
+    chi = ((obs[keep] - exp[keep]) ** 2 / exp[keep]).sum()
+    dof = max(1, keep.sum() - 1)
+    assert stats.chi2.sf(chi, dof) > 1e-3
+    assert abs(x.mean() - m) < 5 * sd / np.sqrt(N)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("k", [0.3, 1.0, 2.5, 25.0, 99.0, 400.0])
+def test_gamma_ks(oracle, dtype, k):
+    x, st = oracle.sample("gamma", 50000, seed=3, k=k, dtype=dtype)
+    assert st == 0
+    assert stats.kstest(x.astype(np.float64), stats.gamma(k).cdf).pvalue > 1e-3
+
+
+def test_gamma_tiny_shape_mean(oracle):
+    x, _ = oracle.sample("gamma", 200000, seed=5, k=1e-3)
+    assert abs(x.mean() - 1e-3) < 5 * np.sqrt(1e-3 / 200000)
+
+
+def test_normal_ks(oracle):
+    for dt in (np.float64, np.float32):
+        x, _ = oracle.sample("normal", 50000, seed=9, dtype=dt)
+        assert stats.kstest(x.astype(np.float64), "norm").pvalue > 1e-3
+
+
+def test_gauss100_switches(oracle):
+    # above 100 the REF_GAUSS100 sampler is N(m, m) truncated to an integer (multiSPDP.cpp:2922-2927)
+    x, _ = oracle.sample("poisson", 50000, seed=1, m=400.0, sampler=oracle.SAMPLER_REF_GAUSS100)
+    z = (x - 400.0) / 20.0
+    assert stats.kstest(z + 0.5 / 20.0, "norm").pvalue > 1e-4 or abs(z.mean()) < 0.05
+    g, _ = oracle.sample("gamma", 50000, seed=2, k=250.0, sampler=oracle.SAMPLER_REF_GAUSS100)
+    assert stats.kstest((g - 250.0) / np.sqrt(250.0), "norm").pvalue > 1e-3
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_dornic_kernel_moments(oracle, dtype):
+    """E[rho*] = e^{beta dt} rho + alpha (e^{beta dt}-1)/beta: the noise-off limit of the Dornic kernel."""
+    c = oracle.dornic_consts(0.72, 1.0, 1.0, 0.1, 1.0)
+    rho, alpha = 0.8, 2.4
+    m = c["pm"] * rho
+    mu1 = alpha * 2.0
+    x, st = oracle.sample("dornic", 200000, seed=4, m=m, mu1=mu1, inv_lambda=c["inv_lambda"], dtype=dtype)
+    assert st == 0
+    mean = c["mean_a1"] * rho + c["mean_a2"] * alpha
+    # Var[rho*] = (mu1 + 2 m)/lambda^2 for Gamma(mu1 + Poisson(m))/lambda
+    var = (mu1 + 2 * m) * c["inv_lambda"] ** 2
+    assert abs(x.mean() - mean) < 5 * np.sqrt(var / len(x))
+    assert abs(x.var() / var - 1) < 0.02
+
+
+def test_determinism_and_precision_consistency(oracle):
+    rng = np.random.default_rng(0)
+    rho = (1 + rng.uniform(-0.01, 0.01, (16, 16)))
+    p = oracle.dp_params()
+    a1, _ = oracle.dp_step(p, rho, 5, 3)
+    a2, _ = oracle.dp_step(p, rho, 5, 3)
+    assert np.array_equal(a1, a2)
+    b1, _ = oracle.dp_step(p, rho, 6, 3)
+    assert not np.array_equal(a1, b1)
+    # noise-off: the step is the conditional mean followed by the exact -b rho^2 flow
+    po = oracle.dp_params(sampler=oracle.SAMPLER_OFF)
+    m64, _ = oracle.dp_step(po, rho, 0, 0)
+    m32, _ = oracle.dp_step(po, rho.astype(np.float32), 0, 0)
+    np.testing.assert_allclose(m32, m64, rtol=1e-6)

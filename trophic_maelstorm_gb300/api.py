@@ -1,0 +1,327 @@
+"""Host-side API over libtm.so, mirroring the reference's interface.
+
+Reference call shape (simulations/Percolation_FD/stochasticSPDP.cpp:940):
+
+    percolationDornic_2D(Rho, t_meas, Rh0, t_max, a, b, D, sigma, dt, dx, r, g)
+
+appends rows {a, L, t, <<rho>_x>_r, Var, #surviving runs, #active sites, #surv alt}
+for t = 0, dt, ... <= 1 and for every t in t_meas.  `percolation_dornic_2d`
+below takes the same arguments (plus a seed and a precision) and returns the
+same rows, computed by one batched GPU run of all r replicates.
+`critical_exp_delta` is the a-sweep around it (stochasticSPDP.cpp:1309-1422),
+`rietkerk_dornic_2d` the Rietkerk counterpart (rietkerk_bjork_FKE.cpp:3697).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib as T
+
+
+# ------------------------------------------------------------------ time grids
+def linspace(start, end, num):
+    """numpy-style linspace as the reference writes it (stochasticSPDP.cpp:254-279)."""
+    if num == 0:
+        return []
+    if num == 1:
+        return [float(start)]
+    delta = (float(end) - float(start)) / (num - 1)
+    return [float(start) + delta * i for i in range(num - 1)] + [float(end)]
+
+
+def logarithm10_time_bins(t_max: float, dt: float) -> list[float]:
+    """Measurement times 10^0 .. 10^floor1(log10 t_max), 25 per decade, snapped
+    down to the dt grid and de-duplicated (stochasticSPDP.cpp:336-378)."""
+    out: list[float] = []
+    if t_max <= 1:
+        return out
+    tend_one = math.floor(math.log10(t_max) * 10.0) / 10.0
+    power = 0.0
+    while power <= tend_one:
+        t_raw = math.pow(10, power)
+        q = t_raw / dt
+        t_fin = float(int(q)) * dt  # static_cast<int>(t_raw/dt)*dt
+        if t_fin <= 1.0:
+            t_fin = t_fin + dt
+        if len(out) > 0 and t_fin != out[-1]:
+            out.append(t_fin)
+        elif len(out) == 0:
+            out.append(t_fin)
+        power += 0.04
+    for i in range(len(out) - 1, 0, -1):
+        if out[i] < out[i - 1] + dt / 2.0:
+            del out[i]
+    return out
+
+
+def reference_step_grid(t_meas, dt):
+    """Step indices the reference measures at: every step while t <= 1 and then the
+    step nearest each t in t_meas (stochasticSPDP.cpp:1003-1025, 1118-1122).
+    Returns (steps, times, n_early) with n_early rows of the t <= 1 block."""
+    times = []
+    t = 0.0
+    while t <= 1:
+        times.append(t)
+        t += dt
+    n_early = len(times)
+    times += [float(x) for x in t_meas]
+    steps = [int(round(x / dt)) for x in times]
+    return steps, times, n_early
+
+
+# ------------------------------------------------------------------ context / batch
+class Context:
+    """A CUDA device plus a stream (tm_create)."""
+
+    def __init__(self, device: int = 0):
+        self._h = C.c_void_p()
+        T.check(T.lib().tm_create(C.byref(self._h), device), "tm_create")
+        self.device = device
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def stream(self) -> int:
+        return int(T.lib().tm_stream(self._h) or 0)
+
+    def sync(self):
+        T.check(T.lib().tm_sync(self._h), "tm_sync")
+
+    def close(self):
+        if self._h:
+            T.lib().tm_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
+
+
+def dp_model(b=2.0, c=0.0, D=1.0, sigma=1.0, dt=0.1, dx=1.0, clamp_lo=0.0, clamp_eps=0.0,
+             remainder=T.TM_REM_EULER_EXACT, sampler=T.TM_SAMPLER_EXACT, deterministic=0, stencil=5,
+             integrator=1) -> T.DPModel:
+    return T.DPModel(b, c, D, sigma, dt, dx, clamp_lo, clamp_eps, remainder, sampler, deterministic, stencil,
+                     integrator, 0)
+
+
+def rietkerk_model(alpha=0.2, k2=5.0, W0=0.2, gmax=0.05, k1=5.0, c=10.0, d=0.25, rW=0.2, DP=0.1, DW=0.1, DO=100.0,
+                   sigma=0.5, dt=1e-3, dx=1.0, clamp_lo=0.0, clamp_eps=1e-10, sampler=T.TM_SAMPLER_REF_GAUSS100,
+                   deterministic=0) -> T.RietkerkModel:
+    return T.RietkerkModel(alpha, k2, W0, gmax, k1, c, d, rW, DP, DW, DO, sigma, dt, dx, clamp_lo, clamp_eps, sampler,
+                           deterministic)
+
+
+def instances(Ls, seeds, a, a_step=0.0):
+    n = len(Ls)
+    a = np.broadcast_to(np.asarray(a, dtype=np.float64), (n,))
+    a_step = np.broadcast_to(np.asarray(a_step, dtype=np.float64), (n,))
+    arr = (T.Instance * n)()
+    for k in range(n):
+        arr[k] = T.Instance(int(Ls[k]), 0, int(seeds[k]) & 0xFFFFFFFFFFFFFFFF, float(a[k]), float(a_step[k]))
+    return arr
+
+
+def layout(inst, nf):
+    n = len(inst)
+    off = np.zeros(n, np.int64)
+    fs = np.zeros(n, np.int64)
+    total = T.lib().tm_layout(inst, n, nf, off.ctypes.data_as(C.POINTER(C.c_int64)),
+                              fs.ctypes.data_as(C.POINTER(C.c_int64)))
+    return int(total), off, fs
+
+
+def pack(fields, inst, nf, dtype):
+    """fields[k]: array (nf, L, L) or (L, L) -> packed 1-D buffer in the batch layout."""
+    total, off, fs = layout(inst, nf)
+    buf = np.zeros(total, dtype)
+    for k, f in enumerate(fields):
+        f = np.asarray(f, dtype).reshape(nf, -1)
+        for j in range(nf):
+            buf[off[k] + j * fs[k]: off[k] + j * fs[k] + f.shape[1]] = f[j]
+    return buf
+
+
+def unpack(buf, inst, nf):
+    total, off, fs = layout(inst, nf)
+    out = []
+    for k in range(len(inst)):
+        L = inst[k].L
+        f = np.stack([buf[off[k] + j * fs[k]: off[k] + j * fs[k] + L * L].reshape(L, L) for j in range(nf)])
+        out.append(f if nf > 1 else f[0])
+    return out
+
+
+class Batch:
+    """A device-resident ragged batch of lattice instances (tm_batch_*)."""
+
+    def __init__(self, ctx: Context, model, inst, precision=T.TM_FP64):
+        self.ctx = ctx
+        self.inst = inst
+        self.n = len(inst)
+        self.precision = precision
+        self.dtype = np.float64 if precision == T.TM_FP64 else np.float32
+        self._h = C.c_void_p()
+        L = T.lib()
+        if isinstance(model, T.DPModel):
+            T.check(L.tm_batch_create_dp(ctx.handle, C.byref(model), inst, self.n, precision, C.byref(self._h)),
+                    "tm_batch_create_dp")
+        else:
+            T.check(L.tm_batch_create_rietkerk(ctx.handle, C.byref(model), inst, self.n, precision,
+                                               C.byref(self._h)), "tm_batch_create_rietkerk")
+        self.nf = L.tm_batch_num_fields(self._h)
+        self.obs_width = L.tm_batch_obs_width(self._h)
+        self.total = int(L.tm_batch_total_elems(self._h))
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def step(self) -> int:
+        return int(T.lib().tm_batch_step(self._h))
+
+    def upload(self, fields, step=0):
+        buf = np.ascontiguousarray(fields, self.dtype) if isinstance(fields, np.ndarray) and fields.ndim == 1 \
+            else pack(fields, self.inst, self.nf, self.dtype)
+        assert buf.size == self.total
+        T.check(T.lib().tm_batch_upload(self._h, buf.ctypes.data_as(C.c_void_p), step), "tm_batch_upload")
+
+    def upload_device(self, ptr: int, step=0):
+        T.check(T.lib().tm_batch_upload_device(self._h, C.c_void_p(ptr), step), "tm_batch_upload_device")
+
+    def download_packed(self):
+        buf = np.empty(self.total, self.dtype)
+        T.check(T.lib().tm_batch_download(self._h, buf.ctypes.data_as(C.c_void_p)), "tm_batch_download")
+        return buf
+
+    def download(self):
+        return unpack(self.download_packed(), self.inst, self.nf)
+
+    def snapshot(self, k):
+        L = self.inst[k].L
+        out = np.empty((self.nf, L, L), self.dtype)
+        T.check(T.lib().tm_batch_snapshot(self._h, k, out.ctypes.data_as(C.c_void_p)), "tm_batch_snapshot")
+        return out if self.nf > 1 else out[0]
+
+    def advance(self, n_steps, meas_steps=()):
+        ms = np.ascontiguousarray(meas_steps, np.int64)
+        obs = np.zeros((max(len(ms), 1), self.n, self.obs_width))
+        st = np.zeros(self.n, np.uint32)
+        T.check(T.lib().tm_batch_advance(self._h, int(n_steps), ms.ctypes.data_as(C.POINTER(C.c_int64)), len(ms),
+                                         obs.ctypes.data_as(C.POINTER(C.c_double)),
+                                         st.ctypes.data_as(C.POINTER(C.c_uint32))), "tm_batch_advance")
+        return obs[:len(ms)], st
+
+    def enqueue_steps(self, n_steps):
+        T.check(T.lib().tm_batch_enqueue_steps(self._h, int(n_steps)), "tm_batch_enqueue_steps")
+
+    def set_launch(self, rows_per_task=0, ctas_per_sm=0):
+        T.check(T.lib().tm_batch_set_launch(self._h, rows_per_task, ctas_per_sm), "tm_batch_set_launch")
+
+    def get_launch(self):
+        r, c = C.c_int(), C.c_int()
+        T.check(T.lib().tm_batch_get_launch(self._h, C.byref(r), C.byref(c)), "tm_batch_get_launch")
+        return r.value, c.value
+
+    def autotune(self, steps_per_trial=4):
+        T.check(T.lib().tm_batch_autotune(self._h, steps_per_trial), "tm_batch_autotune")
+        return self.get_launch()
+
+    def close(self):
+        if self._h:
+            T.lib().tm_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
+
+
+def run_dp(ctx, model, inst, init_packed, n_steps, meas_steps, precision):
+    """tm_run_dp: host buffers in, observables/status/final fields out."""
+    ms = np.ascontiguousarray(meas_steps, np.int64)
+    n = len(inst)
+    init = np.ascontiguousarray(init_packed)
+    obs = np.zeros((max(len(ms), 1), n, 2))
+    st = np.zeros(n, np.uint32)
+    fin = np.empty_like(init)
+    T.check(T.lib().tm_run_dp(ctx.handle, C.byref(model), inst, n, precision, init.ctypes.data_as(C.c_void_p),
+                              int(n_steps), ms.ctypes.data_as(C.POINTER(C.c_int64)), len(ms),
+                              obs.ctypes.data_as(C.POINTER(C.c_double)), st.ctypes.data_as(C.POINTER(C.c_uint32)),
+                              fin.ctypes.data_as(C.c_void_p)), "tm_run_dp")
+    return obs[:len(ms)], st, fin
+
+
+# ------------------------------------------------------------------ reference-shaped calls
+def replicate_rows(a, L, times, n_early, mean, active):
+    """Rows {a, L, t, <<rho>_x>_r, Var, #surviving, <#active>_surv, surv_alt} from per-replicate
+    series mean[j, i], active[j, i] (stochasticSPDP.cpp:1078-1142).  The variance is the
+    unbiased sample variance over the surviving replicates (the reference's running
+    formula divides by (1/(r-1)) in integer arithmetic, :202, so its column is not used)."""
+    r = mean.shape[0]
+    rows = []
+    for i, t in enumerate(times):
+        alive = active[:, i] > 0
+        ns = int(alive.sum())
+        mu = float(mean[alive, i].mean()) if ns else 0.0
+        var = float(mean[alive, i].var(ddof=1)) if ns > 1 else 0.0
+        act = float(active[alive, i].mean()) if ns else 0.0
+        alt = float(r) if i < n_early else float(ns)
+        rows.append([a, float(L), float(t), mu, var, float(ns), act, alt])
+    return np.array(rows)
+
+
+def percolation_dornic_2d(t_meas, Rh0, t_max, a, b, D, sigma, dt, dx, r, g, *, seed=0, precision=T.TM_FP64,
+                          ctx: Context | None = None, a_end=None, remainder=T.TM_REM_EULER_EXACT,
+                          sampler=T.TM_SAMPLER_EXACT, clamp_lo=0.0, clamp_eps=0.0, c=0.0):
+    """GPU percolationDornic_2D: r replicates of one g x g lattice, returned as the
+    reference's rows.  Replicate j uses Philox key seed + j (the reference seeds
+    std::mt19937_64 with random_device()+j, :973-976).  a_end gives a linear ramp
+    of a over the run (a(s) = a + (a_end - a) s / n_steps)."""
+    ctx = ctx or Context(0)
+    steps, times, n_early = reference_step_grid(t_meas, dt)
+    n_steps = max(steps)
+    a_step = 0.0 if a_end is None else (a_end - a) / float(n_steps)
+    inst = instances([g] * r, [seed + j for j in range(r)], a, a_step)
+    model = dp_model(b=b, c=c, D=D, sigma=sigma, dt=dt, dx=dx, clamp_lo=clamp_lo, clamp_eps=clamp_eps,
+                     remainder=remainder, sampler=sampler)
+    dtype = np.float64 if precision == T.TM_FP64 else np.float32
+    init = pack([np.asarray(Rh0, np.float64).reshape(g, g)] * r, inst, 1, dtype)
+    obs, st, _ = run_dp(ctx, model, inst, init, n_steps, steps, precision)
+    mean = obs[:, :, 0].T.copy()
+    act = obs[:, :, 1].T.copy()
+    return replicate_rows(a, g, times, n_early, mean, act), st
+
+
+def critical_exp_delta(Rho_0, div, t_max, a_start, a_end, b, D, sigma, dt, dx, r, g, *, seed=0,
+                       precision=T.TM_FP64, ctx: Context | None = None):
+    """The a-sweep of stochasticSPDP.cpp:1309-1422 in one batch: div values of a
+    (linspace), r replicates each, rows concatenated in a order."""
+    ctx = ctx or Context(0)
+    t_meas = logarithm10_time_bins(t_max, dt)
+    steps, times, n_early = reference_step_grid(t_meas, dt)
+    avals = linspace(a_start, a_end, div)
+    Ls, seeds, av = [], [], []
+    for ia, a in enumerate(avals):
+        for j in range(r):
+            Ls.append(g); seeds.append(seed + ia * r + j); av.append(a)
+    inst = instances(Ls, seeds, av)
+    model = dp_model(b=b, D=D, sigma=sigma, dt=dt, dx=dx)
+    dtype = np.float64 if precision == T.TM_FP64 else np.float32
+    init = pack([np.asarray(Rho_0, np.float64).reshape(g, g)] * len(Ls), inst, 1, dtype)
+    obs, st, _ = run_dp(ctx, model, inst, init, max(steps), steps, precision)
+    rows = []
+    for ia, a in enumerate(avals):
+        sl = slice(ia * r, (ia + 1) * r)
+        rows.append(replicate_rows(a, g, times, n_early, obs[:, sl, 0].T, obs[:, sl, 1].T))
+    return np.concatenate(rows), st

@@ -1,0 +1,457 @@
+// tm_device.cuh -- device-side arithmetic of the Dornic step for sm_103a.
+//
+// Counter-based random stream (Philox4x32-10), own elementary functions and
+// the Poisson / Gamma / normal samplers used by the step kernels.  The
+// specification is fixed operation by operation (compile with -fmad=false;
+// every fused multiply-add is an explicit fma()), so a given
+// (seed, site, step) produces the same variates on every GPU and matches the
+// CPU restatement used by the tests bit for bit.
+//
+// Published methods implemented here:
+//   Philox4x32-10  Salmon, Moraes, Dror, Shaw, SC'11 ("as easy as 1, 2, 3")
+//   Poisson m>=10  Hormann 1993, PTRS (transformed rejection with squeeze)
+//   Poisson m<10   inversion from the top of the tail with one 32-bit word
+//   Gamma          Marsaglia & Tsang 2000, with the U^(1/k) boost for k<1
+//   normal         Marsaglia polar method
+//   log / exp      Cody-Waite argument reduction + Taylor series
+// The reference draws the same two distributions from libstdc++
+// (stochasticSPDP.cpp:1054-1059, multiSPDP.cpp:2915-2943).
+#pragma once
+#include <stdint.h>
+
+#define TM_STATUS_NAN_BIT 0x1u
+#define TM_STATUS_NEG_BIT 0x2u
+#define TM_STATUS_CAP_BIT 0x4u
+
+namespace tmg {
+
+// ---------------------------------------------------------------- Philox
+struct U4 { uint32_t x, y, z, w; };
+
+__device__ __forceinline__ U4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                            uint32_t k0, uint32_t k1)
+{
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r > 0) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+        const uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
+        const uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = __umulhi(0xCD9E8D57u, c2);
+        const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    }
+    return U4{c0, c1, c2, c3};
+}
+
+// ---------------------------------------------------------------- precision traits
+template <typename T> struct Tr;
+template <> struct Tr<double> {
+    static __device__ __forceinline__ double fma_(double a, double b, double c) { return fma(a, b, c); }
+    static __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
+    static __device__ __forceinline__ double floor_(double x) { return floor(x); }
+    static __device__ __forceinline__ double trunc_(double x) { return trunc(x); }
+    static __device__ __forceinline__ double rint_(double x) { return rint(x); }
+    static __device__ __forceinline__ double fabs_(double x) { return fabs(x); }
+};
+template <> struct Tr<float> {
+    static __device__ __forceinline__ float fma_(float a, float b, float c) { return fmaf(a, b, c); }
+    static __device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
+    static __device__ __forceinline__ float floor_(float x) { return floorf(x); }
+    static __device__ __forceinline__ float trunc_(float x) { return truncf(x); }
+    static __device__ __forceinline__ float rint_(float x) { return rintf(x); }
+    static __device__ __forceinline__ float fabs_(float x) { return fabsf(x); }
+};
+
+// ---------------------------------------------------------------- elementary functions
+// 2 atanh(s) = 2s + 2s z (1/3 + z/5 + ...), z = s^2, |s| <= 0.1716
+__device__ __forceinline__ double atanh2_series(double s)
+{
+    const double z = s * s;
+    double p = (double)(1.0 / 21.0);
+    p = fma(z, p, (double)(1.0 / 19.0));
+    p = fma(z, p, (double)(1.0 / 17.0));
+    p = fma(z, p, (double)(1.0 / 15.0));
+    p = fma(z, p, (double)(1.0 / 13.0));
+    p = fma(z, p, (double)(1.0 / 11.0));
+    p = fma(z, p, (double)(1.0 / 9.0));
+    p = fma(z, p, (double)(1.0 / 7.0));
+    p = fma(z, p, (double)(1.0 / 5.0));
+    p = fma(z, p, (double)(1.0 / 3.0));
+    p = p * z;
+    const double t = s + s;
+    return fma(t, p, t);
+}
+__device__ __forceinline__ float atanh2_series(float s)
+{
+    const float z = s * s;
+    float p = (float)(1.0 / 11.0);
+    p = fmaf(z, p, (float)(1.0 / 9.0));
+    p = fmaf(z, p, (float)(1.0 / 7.0));
+    p = fmaf(z, p, (float)(1.0 / 5.0));
+    p = fmaf(z, p, (float)(1.0 / 3.0));
+    p = p * z;
+    const float t = s + s;
+    return fmaf(t, p, t);
+}
+
+__device__ __forceinline__ double tm_log(double x)
+{
+    if (x != x) return x;
+    if (x < 0.0) return __longlong_as_double(0x7ff8000000000000LL);
+    if (x == 0.0) return -__longlong_as_double(0x7ff0000000000000LL);
+    if (x == __longlong_as_double(0x7ff0000000000000LL)) return x;
+    unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    int be = (int)((bits >> 52) & 0x7ff);
+    int adj = 0;
+    if (be == 0) {
+        const double y = x * 0x1p54;
+        bits = (unsigned long long)__double_as_longlong(y);
+        be = (int)((bits >> 52) & 0x7ff);
+        adj = 54;
+    }
+    int e = be - 1023 - adj;
+    bits = (bits & 0x000fffffffffffffULL) | 0x3ff0000000000000ULL;
+    double m = __longlong_as_double((long long)bits);
+    if (m > 0x1.6a09e667f3bcdp+0) { m = m * 0.5; e = e + 1; }
+    const double f = m - 1.0;
+    const double s = f / (2.0 + f);
+    const double lm = atanh2_series(s);
+    const double fe = (double)e;
+    return fma(fe, 0x1.62e42fee00000p-1, fma(fe, 0x1.a39ef35793c76p-33, lm));
+}
+__device__ __forceinline__ float tm_log(float x)
+{
+    if (x != x) return x;
+    if (x < 0.0f) return __int_as_float(0x7fc00000);
+    if (x == 0.0f) return -__int_as_float(0x7f800000);
+    if (x == __int_as_float(0x7f800000)) return x;
+    uint32_t bits = __float_as_uint(x);
+    int be = (int)((bits >> 23) & 0xff);
+    int adj = 0;
+    if (be == 0) {
+        const float y = x * 0x1p25f;
+        bits = __float_as_uint(y);
+        be = (int)((bits >> 23) & 0xff);
+        adj = 25;
+    }
+    int e = be - 127 - adj;
+    bits = (bits & 0x007fffffu) | 0x3f800000u;
+    float m = __uint_as_float(bits);
+    if (m > 0x1.6a09e6p+0f) { m = m * 0.5f; e = e + 1; }
+    const float f = m - 1.0f;
+    const float s = f / (2.0f + f);
+    const float lm = atanh2_series(s);
+    const float fe = (float)e;
+    return fmaf(fe, 0x1.62ep-1f, fmaf(fe, 0x1.0bfbe8p-15f, lm));
+}
+
+__device__ __forceinline__ double tm_log1p(double x)
+{
+    if (x > -0.29 && x < 0.41) return atanh2_series(x / (2.0 + x));
+    return tm_log(1.0 + x);
+}
+__device__ __forceinline__ float tm_log1p(float x)
+{
+    if (x > (float)(-0.29) && x < (float)(0.41)) return atanh2_series(x / (2.0f + x));
+    return tm_log(1.0f + x);
+}
+
+__device__ __forceinline__ double tm_exp(double x)
+{
+    if (x != x) return x;
+    if (x > 709.782712893384) return __longlong_as_double(0x7ff0000000000000LL);
+    if (x < -745.1332191019411) return 0.0;
+    const double k = rint(x * 0x1.71547652b82fep+0);
+    double r = fma(-k, 0x1.62e42fee00000p-1, x);
+    r = fma(-k, 0x1.a39ef35793c76p-33, r);
+    double p = (double)(1.0 / 6227020800.0);
+    p = fma(r, p, (double)(1.0 / 479001600.0));
+    p = fma(r, p, (double)(1.0 / 39916800.0));
+    p = fma(r, p, (double)(1.0 / 3628800.0));
+    p = fma(r, p, (double)(1.0 / 362880.0));
+    p = fma(r, p, (double)(1.0 / 40320.0));
+    p = fma(r, p, (double)(1.0 / 5040.0));
+    p = fma(r, p, (double)(1.0 / 720.0));
+    p = fma(r, p, (double)(1.0 / 120.0));
+    p = fma(r, p, (double)(1.0 / 24.0));
+    p = fma(r, p, (double)(1.0 / 6.0));
+    p = fma(r, p, 0.5);
+    p = fma(r, p, 1.0);
+    p = fma(r, p, 1.0);
+    const int ki = (int)k;
+    const int k1 = ki / 2, k2 = ki - k1;
+    const double s1 = __longlong_as_double((long long)((unsigned long long)(k1 + 1023) << 52));
+    const double s2 = __longlong_as_double((long long)((unsigned long long)(k2 + 1023) << 52));
+    return (p * s1) * s2;
+}
+__device__ __forceinline__ float tm_exp(float x)
+{
+    if (x != x) return x;
+    if (x > 88.72283f) return __int_as_float(0x7f800000);
+    if (x < -103.972084f) return 0.0f;
+    const float k = rintf(x * 0x1.715476p+0f);
+    float r = fmaf(-k, 0x1.62ep-1f, x);
+    r = fmaf(-k, 0x1.0bfbe8p-15f, r);
+    float p = (float)(1.0 / 5040.0);
+    p = fmaf(r, p, (float)(1.0 / 720.0));
+    p = fmaf(r, p, (float)(1.0 / 120.0));
+    p = fmaf(r, p, (float)(1.0 / 24.0));
+    p = fmaf(r, p, (float)(1.0 / 6.0));
+    p = fmaf(r, p, 0.5f);
+    p = fmaf(r, p, 1.0f);
+    p = fmaf(r, p, 1.0f);
+    const int ki = (int)k;
+    const int k1 = ki / 2, k2 = ki - k1;
+    const float s1 = __uint_as_float((uint32_t)(k1 + 127) << 23);
+    const float s2 = __uint_as_float((uint32_t)(k2 + 127) << 23);
+    return (p * s1) * s2;
+}
+
+// 1 - e^-m for m >= 0 (alternating series below 0.25)
+__device__ __forceinline__ double tm_negexpm1(double m)
+{
+    if (m < 0.25) {
+        double p = (double)(1.0 / 6227020800.0);
+        p = fma(m, p, (double)(-1.0 / 479001600.0));
+        p = fma(m, p, (double)(1.0 / 39916800.0));
+        p = fma(m, p, (double)(-1.0 / 3628800.0));
+        p = fma(m, p, (double)(1.0 / 362880.0));
+        p = fma(m, p, (double)(-1.0 / 40320.0));
+        p = fma(m, p, (double)(1.0 / 5040.0));
+        p = fma(m, p, (double)(-1.0 / 720.0));
+        p = fma(m, p, (double)(1.0 / 120.0));
+        p = fma(m, p, (double)(-1.0 / 24.0));
+        p = fma(m, p, (double)(1.0 / 6.0));
+        p = fma(m, p, -0.5);
+        p = fma(m, p, 1.0);
+        return m * p;
+    }
+    return 1.0 - tm_exp(-m);
+}
+__device__ __forceinline__ float tm_negexpm1(float m)
+{
+    if (m < 0.25f) {
+        float p = (float)(-1.0 / 40320.0);
+        p = fmaf(m, p, (float)(1.0 / 5040.0));
+        p = fmaf(m, p, (float)(-1.0 / 720.0));
+        p = fmaf(m, p, (float)(1.0 / 120.0));
+        p = fmaf(m, p, (float)(-1.0 / 24.0));
+        p = fmaf(m, p, (float)(1.0 / 6.0));
+        p = fmaf(m, p, -0.5f);
+        p = fmaf(m, p, 1.0f);
+        return m * p;
+    }
+    return 1.0f - tm_exp(-m);
+}
+
+// ---------------------------------------------------------------- stream
+// Counter (site, step_lo, call, step_hi), key (seed_lo, seed_hi).  Words are
+// consumed in order; a shift register keeps them in registers.
+template <typename T>
+struct Stream {
+    uint32_t k0, k1, site, slo, shi, call;
+    uint32_t b0, b1, b2, b3;
+    int avail;
+    int has_spare;
+    T spare;
+    uint32_t status;
+
+    __device__ __forceinline__ void init(uint64_t seed, uint32_t site_, int64_t step)
+    {
+        k0 = (uint32_t)seed; k1 = (uint32_t)(seed >> 32);
+        site = site_; slo = (uint32_t)(uint64_t)step; shi = (uint32_t)((uint64_t)step >> 32);
+        call = 0; avail = 0; has_spare = 0; spare = T(0); status = 0;
+        b0 = b1 = b2 = b3 = 0;
+    }
+    __device__ __forceinline__ uint32_t u32()
+    {
+        if (avail == 0) {
+            const U4 r = philox4x32_10(site, slo, call, shi, k0, k1);
+            b0 = r.x; b1 = r.y; b2 = r.z; b3 = r.w;
+            call += 1u;
+            avail = 4;
+        }
+        const uint32_t w = b0;
+        b0 = b1; b1 = b2; b2 = b3;
+        --avail;
+        return w;
+    }
+    // uniform on (0,1)
+    __device__ __forceinline__ T open();
+    __device__ __forceinline__ T normal()
+    {
+        if (has_spare) { has_spare = 0; return spare; }
+        for (int it = 0; it < 64; ++it) {
+            const T u = T(2) * open() - T(1);
+            const T v = T(2) * open() - T(1);
+            const T s = u * u + v * v;
+            if (s < T(1) && s > T(0)) {
+                const T f = Tr<T>::sqrt_((T(-2) * tm_log(s)) / s);
+                spare = v * f; has_spare = 1;
+                return u * f;
+            }
+        }
+        status |= TM_STATUS_CAP_BIT;
+        return T(0);
+    }
+};
+template <> __device__ __forceinline__ double Stream<double>::open()
+{
+    const uint32_t w1 = u32();
+    const uint32_t w2 = u32();
+    const unsigned long long x = ((unsigned long long)w1 << 21) | (unsigned long long)(w2 >> 11);
+    return ((double)x + 0.5) * 0x1p-53;
+}
+template <> __device__ __forceinline__ float Stream<float>::open()
+{
+    const uint32_t w = u32();
+    return ((float)(w >> 8) + 0.5f) * 0x1p-24f;
+}
+
+// log k!, k < 16
+__device__ __forceinline__ double logfact_small(int k)
+{
+    switch (k) {
+    case 2: return 0x1.62e42fefa39efp-1;
+    case 3: return 0x1.cab0bfa2a2002p+0;
+    case 4: return 0x1.96ca77c922cf9p+1;
+    case 5: return 0x1.326643c4479c9p+2;
+    case 6: return 0x1.a51273acf01cap+2;
+    case 7: return 0x1.10ce1f32dcc30p+3;
+    case 8: return 0x1.5358e82fcb70dp+3;
+    case 9: return 0x1.99a8921a7f7cfp+3;
+    case 10: return 0x1.e357590954d15p+3;
+    case 11: return 0x1.180973f3a8d74p+4;
+    case 12: return 0x1.3fcba16d50143p+4;
+    case 13: return 0x1.68d5a9c3b32cep+4;
+    case 14: return 0x1.930f3df162a42p+4;
+    case 15: return 0x1.be636a63fd346p+4;
+    default: return 0.0;
+    }
+}
+
+// ---------------------------------------------------------------- samplers
+template <typename T>
+__device__ __forceinline__ T poisson_exact(Stream<T>& g, T m)
+{
+    if (!(m > T(0))) return T(0);
+    if (m < T(10)) {
+        const uint32_t w = g.u32();
+        const T u = (T)w * T(0x1p-32);
+        T p = tm_exp(-m);
+        T q = tm_negexpm1(m);
+        T n = T(0);
+        int it = 0;
+        while (u < q && it < 200) {
+            n = n + T(1);
+            p = (p * m) / n;
+            q = q - p;
+            ++it;
+        }
+        return n;
+    }
+    const T slam = Tr<T>::sqrt_(m);
+    const T loglam = tm_log(m);
+    const T b = T(0.931) + T(2.53) * slam;
+    const T a = T(-0.059) + T(0.02483) * b;
+    const T invalpha = T(1.1239) + T(1.1328) / (b - T(3.4));
+    const T vr = T(0.9277) - T(3.6224) / (b - T(2));
+    const T loginvalpha = tm_log(invalpha);
+    for (int it = 0; it < 64; ++it) {
+        const T U = g.open() - T(0.5);
+        const T V = g.open();
+        const T us = T(0.5) - Tr<T>::fabs_(U);
+        const T k = Tr<T>::floor_((T(2) * a / us + b) * U + m + T(0.43));
+        if (us >= T(0.07) && V <= vr) return k;
+        if (k < T(0) || (us < T(0.013) && V > us)) continue;
+        const T lhs = (tm_log(V) + loginvalpha) - tm_log(a / (us * us) + b);
+        T rhs;
+        if (k < T(16)) {
+            rhs = (k * loglam - m) - (T)logfact_small((int)k);
+        } else {
+            const T z = k + T(1);
+            const T d = z - m;
+            const T iz = T(1) / z;
+            const T iz2 = iz * iz;
+            const T corr = iz * (T(1.0 / 12.0) - iz2 * (T(1.0 / 360.0) - iz2 * T(1.0 / 1260.0)));
+            rhs = ((d - k * tm_log1p(d / m)) - T(0.5) * tm_log(z)) - (T(0x1.d67f1c864beb4p-1) + corr);
+        }
+        if (lhs <= rhs) return k;
+    }
+    g.status |= TM_STATUS_CAP_BIT;
+    return Tr<T>::floor_(m);
+}
+
+template <typename T>
+__device__ __forceinline__ T gamma_mt(Stream<T>& g, T k)
+{
+    if (!(k > T(0))) return T(0);
+    const T kk = (k < T(1)) ? k + T(1) : k;
+    const T d = kk - T(1.0 / 3.0);
+    const T c = T(1) / Tr<T>::sqrt_(T(9) * d);
+    T res = kk;
+    bool done = false;
+    for (int it = 0; it < 64 && !done; ++it) {
+        T x = T(0), v = T(0);
+        bool ok = false;
+        for (int jt = 0; jt < 64; ++jt) {
+            x = g.normal();
+            v = T(1) + c * x;
+            if (v > T(0)) { ok = true; break; }
+        }
+        if (!ok) break;
+        v = (v * v) * v;
+        const T u = g.open();
+        const T x2 = x * x;
+        if (u < T(1) - T(0.0331) * (x2 * x2)) { res = d * v; done = true; break; }
+        if (tm_log(u) < T(0.5) * x2 + d * ((T(1) - v) + tm_log(v))) { res = d * v; done = true; break; }
+    }
+    if (!done) g.status |= TM_STATUS_CAP_BIT;
+    if (k < T(1)) {
+        const T u = g.open();
+        res = res * tm_exp(tm_log(u) / k);
+    }
+    return res;
+}
+
+// sampler: 0 exact, 1 Gaussian above 100 (multiSPDP.cpp:2915-2943)
+template <typename T>
+__device__ __forceinline__ T poisson_draw(Stream<T>& g, T m, int sampler)
+{
+    if (!(m > T(0))) return T(0);
+    if (sampler == 1 && m > T(100)) {
+        const T z = g.normal();
+        return Tr<T>::trunc_(z * Tr<T>::sqrt_(m) + m);
+    }
+    return poisson_exact(g, m);
+}
+
+template <typename T>
+__device__ __forceinline__ T gamma_draw(Stream<T>& g, T k, int sampler)
+{
+    if (sampler == 1 && k > T(100)) {
+        const T z = g.normal();
+        return z * Tr<T>::sqrt_(k) + k;
+    }
+    return gamma_mt(g, k);
+}
+
+// rho* = Gamma(mu1 + Poisson(m)) / lambda  (stochasticSPDP.cpp:1053-1059)
+template <typename T>
+__device__ __forceinline__ T dornic_draw(Stream<T>& g, T m, T mu1, T inv_lambda, int sampler)
+{
+    const T n = poisson_draw(g, m, sampler);
+    const T k = mu1 + n;
+    const T gv = gamma_draw(g, k, sampler);
+    return gv * inv_lambda;
+}
+
+template <typename T>
+__device__ __forceinline__ uint32_t value_status(T x)
+{
+    uint32_t s = 0;
+    if (!(x == x) || Tr<T>::fabs_(x) == T(INFINITY)) s |= TM_STATUS_NAN_BIT;
+    if (x < T(0)) s |= TM_STATUS_NEG_BIT;
+    return s;
+}
+
+}  // namespace tmg

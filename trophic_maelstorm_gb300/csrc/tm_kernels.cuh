@@ -1,0 +1,82 @@
+// tm_kernels.cuh -- kernel parameter blocks and launchers shared by the
+// kernel translation units and the C ABI implementation.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace tmg {
+
+// Dornic constants of one instance: lambda e^{beta dt}, 1/lambda, e^{beta dt}, (e^{beta dt}-1)/beta
+struct __align__(16) Dc4 { double x, y, z, w; };
+
+// Per-instance tables in device memory (structure of arrays).
+struct InstTables {
+    const long long* off;          // element offset of the instance's first field
+    const long long* fstride;      // elements between fields of one instance
+    const int* L;
+    const unsigned long long* seed;
+    const double* R;               // Rietkerk rainfall (per instance)
+    const Dc4* consts;         // Dornic constants: (lambda e^{beta dt}, 1/lambda, e^{beta dt}, (e^{beta dt}-1)/beta)
+    int* alive;                    // DP extinction flags (nullptr: never skip)
+    unsigned* status;              // TM_STATUS_* bits
+};
+
+// Warp task: 32 columns x `rows` rows of one instance: (inst, x0, y0, rows).
+// Block task (RK4 tile): (inst, x0, y0, 0).
+
+template <typename T>
+struct DornicArgs {
+    const T* in;                   // state (field 0 is read)
+    T* out;                        // field-0 slots receive the result
+    InstTables it;
+    const int4* tasks;
+    int n_tasks;
+    const long long* step_base;    // device step counter (graph replays) or nullptr
+    long long step_off;            // step = (*step_base) + step_off
+    T dcoef, two_s2, b, c, dt, dt2, dt6, clo, ceps;
+    int sampler;                   // 0 exact, 1 Gaussian above 100, 2 mean (noise off)
+    int cubic;
+};
+
+template <typename T>
+struct RK4Args {
+    const T* in;                   // [P|W|O] state
+    const T* pstar;                // P after the Dornic draw (field-0 slots); nullptr when deterministic
+    T* out;
+    InstTables it;
+    const int4* tasks;             // block tasks
+    int n_tasks;
+    T alpha, k2, k2W0, gmax, cgmax, k1, rW, d, DPx, DWx, DOx, dt2, dt6, dt, clo, ceps;
+};
+
+template <typename T>
+struct DetStageArgs {              // noise-off DP stage (one instance per launch)
+    const T* x0; const T* kprev; T* kout;
+    int L; T coef;                 // stage input = x0 + coef * kprev
+    T a, b, c, dlap, dk12; int cubic, stencil;
+};
+
+// launchers (defined in the kernel translation units)
+template <typename T>
+cudaError_t launch_dornic(const DornicArgs<T>& a, int rem, int grid, int block, cudaStream_t s);
+template <typename T>
+cudaError_t launch_rk4(const RK4Args<T>& a, bool det, int grid, cudaStream_t s);
+template <typename T>
+cudaError_t launch_measure(const T* state, const InstTables& it, const int4* tasks, int n_tasks, int nf,
+                           double* partial, int grid, int block, cudaStream_t s);
+cudaError_t launch_finalize(const double* partial, const int* task_begin, const InstTables& it, int n_inst, int nf,
+                            int dp_extinction, double* obs_row, cudaStream_t s);
+cudaError_t launch_consts(const double* a0, const double* astep, int n, double diff4, double sigma2, double dt,
+                          const long long* step_base, long long step_off, Dc4* out, cudaStream_t s);
+cudaError_t launch_set_step(long long* d_step, long long v, cudaStream_t s);
+template <typename T>
+cudaError_t launch_det_stage(const DetStageArgs<T>& a, cudaStream_t s);
+template <typename T>
+cudaError_t launch_det_final(const T* x0, const T* k1, const T* k2, const T* k3, const T* k4, T* out, long long n,
+                             T dt, T dt6, int rk4, cudaStream_t s);
+
+constexpr int RK_TX = 32, RK_TY = 16, RK_H = 4;
+constexpr int RK_RX = RK_TX + 2 * RK_H, RK_RY = RK_TY + 2 * RK_H, RK_RN = RK_RX * RK_RY;
+constexpr int RK_THREADS = 256;
+
+}  // namespace tmg

@@ -1,0 +1,117 @@
+// tm_measure.cu -- observables in FP64 with a fixed reduction order.
+//
+// mean_of_vector / occupied_sites_of_vector (stochasticSPDP.cpp:123-154) for
+// every instance of a batch: one warp per task sums its strip (lanes own
+// columns, rows in order), a butterfly of shuffles combines the lanes, and
+// the per-task partials are summed per instance by one warp in task order.
+// No atomics, so a given state always gives the same bits.
+#include "tm_device.cuh"
+#include "tm_kernels.cuh"
+
+namespace tmg {
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// partial[t*4 + f]: f = 0..nf-1 field sums, 3 = sites with field 0 > 0
+template <typename T>
+__global__ void __launch_bounds__(256) measure_kernel(const T* state, const InstTables it, const int4* tasks,
+                                                      int n_tasks, int nf, double* partial)
+{
+    const int lane = threadIdx.x & 31;
+    const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int nw = (int)((gridDim.x * blockDim.x) >> 5);
+    for (int t = gw; t < n_tasks; t += nw) {
+        const int4 tk = tasks[t];
+        const int k = tk.x;
+        const int L = it.L[k];
+        const int x = tk.y + lane;
+        double s0 = 0.0, s1 = 0.0, s2 = 0.0, ac = 0.0;
+        if (x < L && (it.alive == nullptr || it.alive[k] != 0)) {
+            const T* base = state + it.off[k];
+            const long long fs = it.fstride[k];
+            for (int r = 0; r < tk.w; ++r) {
+                const long long i = (long long)(tk.z + r) * L + x;
+                const T v = base[i];
+                s0 += (double)v;
+                if (v > T(0)) ac += 1.0;
+                if (nf == 3) {
+                    s1 += (double)base[i + fs];
+                    s2 += (double)base[i + 2 * fs];
+                }
+            }
+        }
+        s0 = warp_sum(s0);
+        ac = warp_sum(ac);
+        if (nf == 3) { s1 = warp_sum(s1); s2 = warp_sum(s2); }
+        if (lane == 0) {
+            partial[4LL * t + 0] = s0;
+            partial[4LL * t + 1] = s1;
+            partial[4LL * t + 2] = s2;
+            partial[4LL * t + 3] = ac;
+        }
+    }
+}
+
+template <typename T>
+cudaError_t launch_measure(const T* state, const InstTables& it, const int4* tasks, int n_tasks, int nf,
+                           double* partial, int grid, int block, cudaStream_t s)
+{
+    if (n_tasks <= 0) return cudaSuccess;
+    measure_kernel<T><<<grid, block, 0, s>>>(state, it, tasks, n_tasks, nf, partial);
+    return cudaGetLastError();
+}
+template cudaError_t launch_measure<float>(const float*, const InstTables&, const int4*, int, int, double*, int, int,
+                                           cudaStream_t);
+template cudaError_t launch_measure<double>(const double*, const InstTables&, const int4*, int, int, double*, int,
+                                            int, cudaStream_t);
+
+// One warp per instance: obs_row[k*W + f], W = 2 (DP: mean, active) or 4
+// (Rietkerk: mean P, W, O, active P).  With dp_extinction, an instance seen with
+// no active site is marked extinct (stochasticSPDP.cpp:1021-1022).
+__global__ void finalize_kernel(const double* partial, const int* task_begin, const InstTables it, int n_inst, int nf,
+                                int dp_extinction, double* obs_row)
+{
+    const int lane = threadIdx.x & 31;
+    const int k = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (k >= n_inst) return;
+    const int t0 = task_begin[k], t1 = task_begin[k + 1];
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, ac = 0.0;
+    for (int t = t0 + lane; t < t1; t += 32) {
+        s0 += partial[4LL * t + 0];
+        s1 += partial[4LL * t + 1];
+        s2 += partial[4LL * t + 2];
+        ac += partial[4LL * t + 3];
+    }
+    s0 = warp_sum(s0); s1 = warp_sum(s1); s2 = warp_sum(s2); ac = warp_sum(ac);
+    if (lane == 0) {
+        const bool dead = it.alive != nullptr && it.alive[k] == 0;
+        const double n = (double)it.L[k] * (double)it.L[k];
+        if (nf == 1) {
+            obs_row[2LL * k + 0] = dead ? 0.0 : s0 / n;
+            obs_row[2LL * k + 1] = dead ? 0.0 : ac;
+        } else {
+            obs_row[4LL * k + 0] = s0 / n;
+            obs_row[4LL * k + 1] = s1 / n;
+            obs_row[4LL * k + 2] = s2 / n;
+            obs_row[4LL * k + 3] = ac;
+        }
+        if (dp_extinction && it.alive != nullptr && ac == 0.0) it.alive[k] = 0;
+    }
+}
+
+cudaError_t launch_finalize(const double* partial, const int* task_begin, const InstTables& it, int n_inst, int nf,
+                            int dp_extinction, double* obs_row, cudaStream_t s)
+{
+    if (n_inst <= 0) return cudaSuccess;
+    const int threads = 256;
+    const int grid = (n_inst * 32 + threads - 1) / threads;
+    finalize_kernel<<<grid, threads, 0, s>>>(partial, task_begin, it, n_inst, nf, dp_extinction, obs_row);
+    return cudaGetLastError();
+}
+
+}  // namespace tmg

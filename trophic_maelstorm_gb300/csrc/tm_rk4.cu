@@ -1,0 +1,212 @@
+// tm_rk4.cu -- RK4 of the Rietkerk three-field right-hand side, fused in one
+// pass over a shared-memory tile, and the noise-off DP stage kernels.
+//
+// Rietkerk (rietkerk_bjork_FKE.cpp:2363-2444 stochastic remainder f_2Dor,
+// :1760-1856 noise-off f_2D): the W and O tendencies carry 5-point
+// Laplacians, so stage s needs stage s-1 values one site further out.  A CTA
+// loads a (32+8) x (16+8) region of [P*, W, O] (halo 4, periodic wrap) into
+// shared memory and runs all four stages there, each stage valid on a region
+// one site smaller, so the 32 x 16 interior comes out exact after stage 4.
+// The state is read and written once per step (plus the halo re-read, which
+// hits L2); the K1..K4 temporaries the reference keeps as full lattices
+// never leave the SM.
+#include "tm_device.cuh"
+#include "tm_kernels.cuh"
+
+namespace tmg {
+
+template <typename T, bool DET>
+__global__ void __launch_bounds__(RK_THREADS) rk4_tile_kernel(const RK4Args<T> A)
+{
+    __shared__ T X0[3][RK_RN];
+    __shared__ T M[3][RK_RN];
+    constexpr int PER = (RK_RN + RK_THREADS - 1) / RK_THREADS;
+    const int tid = threadIdx.x;
+    for (int t = blockIdx.x; t < A.n_tasks; t += gridDim.x) {
+        const int4 tk = A.tasks[t];
+        const int k = tk.x;
+        const int L = A.it.L[k];
+        const long long off = A.it.off[k];
+        const long long fs = A.it.fstride[k];
+        const T R = (T)A.it.R[k];
+        const int x0 = tk.y, y0 = tk.z;
+        const T* __restrict__ P0 = (DET ? A.in : A.pstar) + off;
+        const T* __restrict__ W0 = A.in + off + fs;
+        const T* __restrict__ O0 = A.in + off + 2 * fs;
+        __syncthreads();  // previous task finished with the tile
+        for (int c = tid; c < RK_RN; c += RK_THREADS) {
+            const int ry = c / RK_RX, rx = c - ry * RK_RX;
+            int gy = (y0 - RK_H + ry) % L; if (gy < 0) gy += L;
+            int gx = (x0 - RK_H + rx) % L; if (gx < 0) gx += L;
+            const long long gi = (long long)gy * L + gx;
+            X0[0][c] = P0[gi];
+            X0[1][c] = W0[gi];
+            X0[2][c] = O0[gi];
+        }
+        __syncthreads();
+        T acc[PER][3];
+        T kv[PER][3];
+#pragma unroll
+        for (int j = 0; j < PER; ++j) { acc[j][0] = acc[j][1] = acc[j][2] = T(0); }
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+            const T (*S)[RK_RN] = (s == 0) ? X0 : M;
+#pragma unroll
+            for (int j = 0; j < PER; ++j) {
+                const int c = tid + j * RK_THREADS;
+                kv[j][0] = kv[j][1] = kv[j][2] = T(0);
+                if (c < RK_RN) {
+                    const int ry = c / RK_RX, rx = c - ry * RK_RX;
+                    if (ry >= 1 && ry < RK_RY - 1 && rx >= 1 && rx < RK_RX - 1) {
+                        const int cn = c - RK_RX, cs = c + RK_RX, cw = c - 1, ce = c + 1;
+                        const T Pc = S[0][c], Wc = S[1][c], Oc = S[2][c];
+                        const T upt_num = (A.gmax * Wc) * Pc;
+                        const T wk = Wc + A.k1;
+                        const T infil = ((A.alpha * (Pc + A.k2W0)) / (Pc + A.k2)) * Oc;
+                        const T lapW = (((S[1][cn] + S[1][cs]) + S[1][cw]) + S[1][ce]) - T(4) * Wc;
+                        const T lapO = (((S[2][cn] + S[2][cs]) + S[2][cw]) + S[2][ce]) - T(4) * Oc;
+                        T fP = ((A.cgmax * Wc) * Pc) / wk;
+                        if (DET) {
+                            const T lapP = (((S[0][cn] + S[0][cs]) + S[0][cw]) + S[0][ce]) - T(4) * Pc;
+                            fP = (fP - A.d * Pc) + A.DPx * lapP;
+                        }
+                        kv[j][0] = fP;
+                        kv[j][1] = ((infil - upt_num / wk) - A.rW * Wc) + A.DWx * lapW;
+                        kv[j][2] = (R - infil) + A.DOx * lapO;
+                    }
+                    if (s == 0) {
+                        acc[j][0] = kv[j][0]; acc[j][1] = kv[j][1]; acc[j][2] = kv[j][2];
+                    } else if (s == 3) {
+                        acc[j][0] = acc[j][0] + kv[j][0]; acc[j][1] = acc[j][1] + kv[j][1]; acc[j][2] = acc[j][2] + kv[j][2];
+                    } else {
+                        acc[j][0] = acc[j][0] + T(2) * kv[j][0];
+                        acc[j][1] = acc[j][1] + T(2) * kv[j][1];
+                        acc[j][2] = acc[j][2] + T(2) * kv[j][2];
+                    }
+                }
+            }
+            if (s < 3) {
+                const T coef = (s == 2) ? A.dt : A.dt2;
+                __syncthreads();  // all reads of the stage input done
+#pragma unroll
+                for (int j = 0; j < PER; ++j) {
+                    const int c = tid + j * RK_THREADS;
+                    if (c < RK_RN) {
+                        M[0][c] = X0[0][c] + coef * kv[j][0];
+                        M[1][c] = X0[1][c] + coef * kv[j][1];
+                        M[2][c] = X0[2][c] + coef * kv[j][2];
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        unsigned st = 0;
+#pragma unroll
+        for (int j = 0; j < PER; ++j) {
+            const int c = tid + j * RK_THREADS;
+            if (c < RK_RN) {
+                const int ry = c / RK_RX, rx = c - ry * RK_RX;
+                const int ly = ry - RK_H, lx = rx - RK_H;
+                const int gy = y0 + ly, gx = x0 + lx;
+                if (ly >= 0 && ly < RK_TY && lx >= 0 && lx < RK_TX && gy < L && gx < L) {
+                    const long long gi = off + (long long)gy * L + gx;
+#pragma unroll
+                    for (int f = 0; f < 3; ++f) {
+                        T v = X0[f][c] + A.dt6 * acc[j][f];
+                        if (v < A.ceps && v >= A.clo) v = T(0);
+                        st |= value_status(v);
+                        A.out[gi + f * fs] = v;
+                    }
+                }
+            }
+        }
+        if (st) atomicOr(A.it.status + k, st);
+    }
+}
+
+template <typename T>
+cudaError_t launch_rk4(const RK4Args<T>& a, bool det, int grid, cudaStream_t s)
+{
+    if (a.n_tasks <= 0) return cudaSuccess;
+    if (det) rk4_tile_kernel<T, true><<<grid, RK_THREADS, 0, s>>>(a);
+    else rk4_tile_kernel<T, false><<<grid, RK_THREADS, 0, s>>>(a);
+    return cudaGetLastError();
+}
+template cudaError_t launch_rk4<float>(const RK4Args<float>&, bool, int, cudaStream_t);
+template cudaError_t launch_rk4<double>(const RK4Args<double>&, bool, int, cudaStream_t);
+
+// ---- noise-off DP: drho/dt = a rho - b rho^2 - c rho^3 + D Lap(rho) ---------------
+// 5-point Laplacian, or the 4th-order cross of fP_2D (stochasticSPDP.cpp:516-529)
+// written as f = react - D/(12 dx^2) (o2 - 16 o1 + 60 rho).  One thread per site;
+// the stage input x0 + coef*kprev is formed on the fly for the site and its
+// neighbours (percNoDiff_2D :594-626).
+template <typename T>
+__device__ __forceinline__ T det_in(const DetStageArgs<T>& A, long long i)
+{
+    return A.kprev ? A.x0[i] + A.coef * A.kprev[i] : A.x0[i];
+}
+
+template <typename T>
+__global__ void det_stage_kernel(const DetStageArgs<T> A)
+{
+    const long long n = (long long)A.L * A.L;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int L = A.L;
+        const int y = (int)(i / L), x = (int)(i - (long long)y * L);
+        const T r = det_in(A, i);
+        T f = (A.a * r) - ((A.b * r) * r);
+        if (A.cubic) f = f - ((A.c * r) * r) * r;
+        if (A.stencil == 5) {
+            const int yn = (y + L - 1) % L, ys = (y + 1) % L, xw = (x + L - 1) % L, xe = (x + 1) % L;
+            const T lap = (((det_in(A, (long long)yn * L + x) + det_in(A, (long long)ys * L + x)) +
+                            det_in(A, (long long)y * L + xw)) + det_in(A, (long long)y * L + xe)) - T(4) * r;
+            f = f + A.dlap * lap;
+        } else {
+            const int ym2 = (y + 2 * L - 2) % L, ym1 = (y + L - 1) % L, yp1 = (y + 1) % L, yp2 = (y + 2) % L;
+            const int xm2 = (x + 2 * L - 2) % L, xm1 = (x + L - 1) % L, xp1 = (x + 1) % L, xp2 = (x + 2) % L;
+            const T o2 = ((det_in(A, (long long)ym2 * L + x) + det_in(A, (long long)yp2 * L + x)) +
+                          det_in(A, (long long)y * L + xm2)) + det_in(A, (long long)y * L + xp2);
+            const T o1 = ((det_in(A, (long long)ym1 * L + x) + det_in(A, (long long)yp1 * L + x)) +
+                          det_in(A, (long long)y * L + xm1)) + det_in(A, (long long)y * L + xp1);
+            const T s = (T(1) * o2 - T(16) * o1) + T(60) * r;
+            f = f - A.dk12 * s;
+        }
+        A.kout[i] = f;
+    }
+}
+
+template <typename T>
+cudaError_t launch_det_stage(const DetStageArgs<T>& a, cudaStream_t s)
+{
+    const long long n = (long long)a.L * a.L;
+    const int grid = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+    det_stage_kernel<T><<<grid, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+template cudaError_t launch_det_stage<float>(const DetStageArgs<float>&, cudaStream_t);
+template cudaError_t launch_det_stage<double>(const DetStageArgs<double>&, cudaStream_t);
+
+template <typename T>
+__global__ void det_final_kernel(const T* x0, const T* k1, const T* k2, const T* k3, const T* k4, T* out, long long n,
+                                 T dt, T dt6, int rk4)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        if (rk4) out[i] = x0[i] + dt6 * (((k1[i] + T(2) * k2[i]) + T(2) * k3[i]) + k4[i]);
+        else out[i] = x0[i] + k1[i] * dt;
+    }
+}
+
+template <typename T>
+cudaError_t launch_det_final(const T* x0, const T* k1, const T* k2, const T* k3, const T* k4, T* out, long long n,
+                             T dt, T dt6, int rk4, cudaStream_t s)
+{
+    const int grid = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+    det_final_kernel<T><<<grid, 256, 0, s>>>(x0, k1, k2, k3, k4, out, n, dt, dt6, rk4);
+    return cudaGetLastError();
+}
+template cudaError_t launch_det_final<float>(const float*, const float*, const float*, const float*, const float*,
+                                             float*, long long, float, float, int, cudaStream_t);
+template cudaError_t launch_det_final<double>(const double*, const double*, const double*, const double*,
+                                              const double*, double*, long long, double, double, int, cudaStream_t);
+
+}  // namespace tmg
