@@ -48,9 +48,13 @@ def a_values():
     return list(np.geomspace(A_CENTER * 0.98, A_CENTER * 1.02, NA))
 
 
-def workload():
+def workload(kind="sweep"):
     Ls, seeds, avs = [], [], []
     k = 0
+    if kind == "l1024x64":  # profiling case: 64 instances of the L=1024 subset (268 MB per state buffer)
+        for r in range(64):
+            Ls.append(1024); seeds.append(1_000_003 * r + 17); avs.append(float(a_values()[r % NA]))
+        return Ls, seeds, avs
     for L in LS:
         for a in a_values():
             for r in range(REPS):
@@ -230,7 +234,7 @@ def run_ours(args):
     ctx = tmg.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream)
 
-    Ls, seeds, avs = workload()
+    Ls, seeds, avs = workload(args.workload)
     # every rank runs the full workload on its own GPU (independent replicas, weak scaling)
     seeds = [s + 7919 * rank for s in seeds]
     inst = tmg.instances(Ls, seeds, avs)
@@ -285,12 +289,15 @@ def run_ours(args):
     obs_bytes = len(meas) * len(Ls) * 2 * 8
     torch.cuda.synchronize()
     barrier(world)
-    t0 = time.perf_counter()
-    b.upload(hv, step=0)
-    obs, st = b.advance(e_steps, [0, e_steps])
-    e2e_s = time.perf_counter() - t0
-    e2e_s = max_over_ranks(e2e_s, world)
-    e2e = sites * e_steps * world / e2e_s
+    st = np.zeros(0, np.uint32)
+    e2e = None
+    if not args.no_e2e:
+        t0 = time.perf_counter()
+        b.upload(hv, step=0)
+        obs, st = b.advance(e_steps, [0, e_steps])
+        e2e_s = time.perf_counter() - t0
+        e2e_s = max_over_ranks(e2e_s, world)
+        e2e = sites * e_steps * world / e2e_s
 
     hbm, peak_kind = peaks()
     avg_launch_s = statistics.mean(per) * 1e-3
@@ -307,7 +314,8 @@ def run_ours(args):
             "value": value, "unit": "site-updates/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "ragged DP Dornic sweep: L in {64..1024} x 32 replicates x 16 a (2560 instances)",
+            "config": {"workload": "ragged DP Dornic sweep: L in {64..1024} x 32 replicates x 16 a (2560 instances)"
+                       if args.workload == "sweep" else f"profiling case {args.workload}",
                        "sites_per_step": sites, "b": 2.0, "D": 1.0, "sigma": 1.0, "dt": 0.1,
                        "a_values": "16 log-spaced in [0.7056, 0.7344]", "init": "1+U(-0.01,0.01), all sites live",
                        "state": "FP32, FP64 reductions", "l2": "inputs larger than L2 (2.86 GB state per buffer)",
@@ -317,8 +325,9 @@ def run_ours(args):
                          "kernel": "dornic_step_kernel<float, euler>", "alg_bytes_per_site": BYTES_PER_SITE_FP32,
                          "avg_launch_ms": avg_launch_s * 1e3},
             "cpu_baseline": cpu,
-            "e2e": {"value": e2e, "unit": "site-updates/s", "h2d_bytes_per_step": total * 4 / e_steps,
-                    "d2h_bytes_per_step": obs_bytes / e_steps, "steps": e_steps},
+            "e2e": None if e2e is None else {"value": e2e, "unit": "site-updates/s",
+                                             "h2d_bytes_per_step": total * 4 / e_steps,
+                                             "d2h_bytes_per_step": obs_bytes / e_steps, "steps": e_steps},
             "gpu_launches": args.steps,
             "clocks": clocks,
             "status_bits": int(np.bitwise_or.reduce(st)) if len(st) else 0,
@@ -338,6 +347,8 @@ def main():
     ap.add_argument("--autotune", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--workload", default="sweep", choices=["sweep", "l1024x64"])
+    ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
