@@ -185,6 +185,36 @@ int tm_run_rietkerk(tm_ctx* ctx, const tm_rietkerk_model* model, const tm_instan
                     int precision, const void* init_fields, int64_t n_steps, const int64_t* meas_steps,
                     int n_meas, double* obs, uint32_t* status, void* final_fields);
 
+/* -- observables without allocation ---------------------------------------
+ * No counterpart in the reference: it exists for callers that cannot let a
+ * library allocate device memory -- for example a host application that has
+ * already given the GPU's memory to its own pool allocator, or a
+ * latency-sensitive loop that must not trigger cudaMalloc's implicit device
+ * synchronisation.  It computes the same FP64 observables as a DP measurement
+ * of tm_batch_advance (spatial mean of rho and the number of sites with
+ * rho > 0, per instance) for lattices that live in the caller's own device
+ * buffer, and writes them to the caller's device buffer dev_out[2*k + {0,1}].
+ * It calls no cudaMalloc/cudaFree: its scratch (instance table, task table,
+ * per-task partial sums) is a static TM_NOALLOC_SCRATCH_BYTES array in the
+ * library image, held by every GPU that loads libtm.so until the process exits.
+ *   dev_fields  device pointer, elements of `precision` (TM_FP64 / TM_FP32)
+ *   L, offsets  host arrays, n_inst entries: lattice side and element offset of
+ *               each instance in dev_fields (e.g. from tm_layout)
+ *   stream      cudaStream_t to run on (NULL: the legacy default stream)
+ * Returns TM_ERR_INVALID when the instances need more scratch than the array
+ * holds: 256-byte-aligned regions of 8*n_inst + 4*n_inst + 4*(n_inst+1) bytes
+ * plus 24 bytes per 32-column strip (sum over instances of ceil(L/32)).
+ * The first call on a device looks up the array's device address (once per
+ * device, with that device current); make that first call before any stream
+ * capture.  All calls share the one array and leave their contents in it;
+ * every value a call reads it has written itself, so nothing needs clearing,
+ * but two calls that overlap on the GPU (other streams, other host threads)
+ * race on the array: order them on one stream or synchronise between them.
+ * The call is asynchronous on `stream`; dev_out is ready when it completes. */
+#define TM_NOALLOC_SCRATCH_BYTES (4u << 20)
+int tm_observe_noalloc(const void* dev_fields, int precision, const int32_t* L, const int64_t* offsets,
+                       int n_inst, double* dev_out, void* stream);
+
 /* Packed-layout geometry without a batch (for callers that pack host buffers
  * before creating one): offsets[k] and the total, for nf fields per instance. */
 int64_t tm_layout(const tm_instance* inst, int n_inst, int nf, int64_t* offsets, int64_t* field_strides);
