@@ -225,6 +225,65 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def plain_fp64(ctx, tmg, torch, args, steps=6):
+    """The plain path the batched sweep is compared with: one FP64 instance at a time,
+    each L of the sweep, timed per step; sweep throughput weights each L by its
+    share of the sweep's instances (all equal)."""
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    rng = np.random.default_rng(1)
+    per_L = {}
+    tot_sites = 0.0
+    tot_time = 0.0
+    for L in LS:
+        inst = tmg.instances([L], [7], A_CENTER)
+        b = tmg.Batch(ctx, tmg.dp_model(**MODEL), inst, tmg.TM_FP64)
+        f0 = (1.0 + rng.uniform(-0.01, 0.01, (L, L)))
+        b.upload([f0])
+        b.enqueue_steps(2)
+        ctx.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for _ in range(steps):
+                b.enqueue_steps(1)
+            e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        per_L[str(L)] = {"ms_per_step": ms, "site_updates_per_s": L * L / (ms * 1e-3)}
+        tot_sites += L * L
+        tot_time += ms * 1e-3
+        b.close()
+    return {"sweep_site_updates_per_s": tot_sites / tot_time, "per_L": per_L,
+            "note": "one FP64 instance per batch, same fully-active start; sweep figure = sum(L^2)/sum(step time)"}
+
+
+def late_regime(ctx, tmg, torch, args, burn=600, steps=10):
+    """Throughput later in the run: the 64 x 1024^2 subset after `burn` steps from the
+    fully-active start (near-critical decay leaves most sites absorbing)."""
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    Ls, seeds, avs = workload("l1024x64")
+    inst = tmg.instances(Ls, seeds, avs)
+    b = tmg.Batch(ctx, tmg.dp_model(**MODEL), inst, tmg.TM_FP32)
+    rng = np.random.default_rng(2)
+    b.upload([init_field(1024, rng) for _ in Ls])
+    b.enqueue_steps(burn)
+    obs, _ = b.advance(0, [b.step])
+    active = float(obs[0, :, 1].sum()) / (len(Ls) * 1024 * 1024)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        for _ in range(steps):
+            b.enqueue_steps(1)
+        e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    sites = len(Ls) * 1024 * 1024
+    b.close()
+    return {"burn_steps": burn, "t": burn * MODEL["dt"], "active_site_fraction": active, "ms_per_step": ms,
+            "site_updates_per_s": sites / (ms * 1e-3),
+            "hbm_frac": BYTES_PER_SITE_FP32 * sites / (ms * 1e-3) / 1e9 / peaks()[0]}
+
+
 def run_ours(args):
     import torch
     import trophic_maelstorm_gb300 as tmg
@@ -299,6 +358,11 @@ def run_ours(args):
         e2e_s = max_over_ranks(e2e_s, world)
         e2e = sites * e_steps * world / e2e_s
 
+    extras = {}
+    if not args.no_extras:
+        extras["plain_fp64_single_instance"] = plain_fp64(ctx, tmg, torch, args)
+        extras["late_regime"] = late_regime(ctx, tmg, torch, args)
+
     hbm, peak_kind = peaks()
     avg_launch_s = statistics.mean(per) * 1e-3
     alg_bytes = BYTES_PER_SITE_FP32 * sites
@@ -331,6 +395,7 @@ def run_ours(args):
             "gpu_launches": args.steps,
             "clocks": clocks,
             "status_bits": int(np.bitwise_or.reduce(st)) if len(st) else 0,
+            "extras": extras,
         }
         print(json.dumps(line), flush=True)
     b.close()
@@ -349,6 +414,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--workload", default="sweep", choices=["sweep", "l1024x64"])
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-extras", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -12,6 +12,8 @@
 #include <omp.h>
 #endif
 
+#include "tm_zig_table.inc"
+
 /* Philox4x32-10: J. K. Salmon, M. A. Moraes, R. O. Dror, D. E. Shaw,
  * "Parallel random numbers: as easy as 1, 2, 3", SC'11.  Ten rounds of
  * (c0,c1,c2,c3) -> (hi(M1 c2)^c1^k0, lo(M1 c2), hi(M0 c0)^c3^k1, lo(M0 c0))

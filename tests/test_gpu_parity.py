@@ -129,7 +129,7 @@ def test_launch_shape_and_path_invariance(tmg, ctx, precision):
     dtype = np.float64 if precision == 0 else np.float32
     init = [f.astype(dtype) for f in _init_fields(Ls, 3)]
     res = []
-    for rows, ctas, chunks in ((32, 4, [70]), (8, 2, [70]), (64, 8, [70]), (16, 1, [1] * 70)):
+    for rows, ctas, chunks in ((8, 4, [70]), (4, 2, [70]), (16, 8, [70]), (16, 1, [1] * 70)):
         b = tmg.Batch(ctx, model, inst, precision)
         b.set_launch(rows, ctas)
         b.upload(init)

@@ -88,7 +88,7 @@ struct tm_batch {
     unsigned* d_status = nullptr;
     bool ramped = false;
 
-    int rows_per_task = 32;
+    int rows_per_task = 8;
     int ctas_per_sm = 4;
     int4* d_tasks = nullptr;
     int n_tasks = 0;
@@ -171,7 +171,7 @@ DornicArgs<T> dornic_args(const tm_batch* b, const T* in, T* out, const long lon
 {
     DornicArgs<T> a{};
     a.in = in; a.out = out; a.it = b->tables(); a.tasks = b->d_tasks; a.n_tasks = b->n_tasks;
-    a.step_base = step_base; a.step_off = step_off;
+    a.step_base = step_base; a.step_off = step_off; a.rows_cap = b->rows_per_task;
     if (b->model == 0) {
         const tm_dp_model& m = b->dpm;
         a.dcoef = (T)(m.D / (m.dx * m.dx));
@@ -694,7 +694,7 @@ int tm_batch_enqueue_steps(tm_batch* b, int64_t n_steps)
 
 int tm_batch_set_launch(tm_batch* b, int rows, int ctas)
 {
-    if (!b || rows < 0 || ctas < 0 || rows > 4096 || ctas > 64) return TM_ERR_INVALID;
+    if (!b || rows < 0 || ctas < 0 || rows > kMaxRowsPerTask || ctas > 64) return TM_ERR_INVALID;
     TM_CUDA(cudaSetDevice(b->ctx->device));
     TM_CUDA(cudaStreamSynchronize(b->ctx->stream));
     bool rebuild = false;
@@ -727,8 +727,8 @@ int tm_batch_autotune(tm_batch* b, int steps_per_trial)
     TM_CUDA(cudaStreamSynchronize(s));
     const int64_t step0 = b->step;
     const int cur0 = b->cur;
-    const int rows_c[] = {8, 16, 32, 64};
-    const int ctas_c[] = {2, 4, 8};
+    const int rows_c[] = {4, 8, 16};
+    const int ctas_c[] = {1, 2, 3, 4};
     int best_r = b->rows_per_task, best_c = b->ctas_per_sm;
     float best = 1e30f;
     cudaEvent_t e0, e1;

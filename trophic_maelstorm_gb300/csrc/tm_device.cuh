@@ -9,15 +9,16 @@
 //
 // Published methods implemented here:
 //   Philox4x32-10  Salmon, Moraes, Dror, Shaw, SC'11 ("as easy as 1, 2, 3")
-//   Poisson m>=10  Hormann 1993, PTRS (transformed rejection with squeeze)
-//   Poisson m<10   inversion from the top of the tail with one 32-bit word
+//   Poisson m>=32  Hormann 1993, PTRS (transformed rejection with squeeze)
+//   Poisson m<32   inversion from the top of the tail with one 32-bit word
 //   Gamma          Marsaglia & Tsang 2000, with the U^(1/k) boost for k<1
-//   normal         Marsaglia polar method
+//   normal         ziggurat (Marsaglia & Tsang 2000), tables from oracle/gen_ziggurat.py
 //   log / exp      Cody-Waite argument reduction + Taylor series
 // The reference draws the same two distributions from libstdc++
 // (stochasticSPDP.cpp:1054-1059, multiSPDP.cpp:2915-2943).
 #pragma once
 #include <stdint.h>
+#include "tm_zig_table.cuh"
 
 #define TM_STATUS_NAN_BIT 0x1u
 #define TM_STATUS_NEG_BIT 0x2u
@@ -144,6 +145,36 @@ __device__ __forceinline__ float tm_log(float x)
     return fmaf(fe, 0x1.62ep-1f, fmaf(fe, 0x1.0bfbe8p-15f, lm));
 }
 
+// log for arguments known to be positive, finite and normal (uniform
+// variates, means, shapes): the same arithmetic as tm_log without the
+// special-case branches, so it returns the same bits for such arguments.
+__device__ __forceinline__ double tm_log_pos(double x)
+{
+    unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    int e = (int)((bits >> 52) & 0x7ff) - 1023;
+    bits = (bits & 0x000fffffffffffffULL) | 0x3ff0000000000000ULL;
+    double m = __longlong_as_double((long long)bits);
+    if (m > 0x1.6a09e667f3bcdp+0) { m = m * 0.5; e = e + 1; }
+    const double f = m - 1.0;
+    const double s = f / (2.0 + f);
+    const double lm = atanh2_series(s);
+    const double fe = (double)e;
+    return fma(fe, 0x1.62e42fee00000p-1, fma(fe, 0x1.a39ef35793c76p-33, lm));
+}
+__device__ __forceinline__ float tm_log_pos(float x)
+{
+    uint32_t bits = __float_as_uint(x);
+    int e = (int)((bits >> 23) & 0xff) - 127;
+    bits = (bits & 0x007fffffu) | 0x3f800000u;
+    float m = __uint_as_float(bits);
+    if (m > 0x1.6a09e6p+0f) { m = m * 0.5f; e = e + 1; }
+    const float f = m - 1.0f;
+    const float s = f / (2.0f + f);
+    const float lm = atanh2_series(s);
+    const float fe = (float)e;
+    return fmaf(fe, 0x1.62ep-1f, fmaf(fe, 0x1.0bfbe8p-15f, lm));
+}
+
 __device__ __forceinline__ double tm_log1p(double x)
 {
     if (x > -0.29 && x < 0.41) return atanh2_series(x / (2.0 + x));
@@ -251,15 +282,13 @@ struct Stream {
     uint32_t k0, k1, site, slo, shi, call;
     uint32_t b0, b1, b2, b3;
     int avail;
-    int has_spare;
-    T spare;
     uint32_t status;
 
     __device__ __forceinline__ void init(uint64_t seed, uint32_t site_, int64_t step)
     {
         k0 = (uint32_t)seed; k1 = (uint32_t)(seed >> 32);
         site = site_; slo = (uint32_t)(uint64_t)step; shi = (uint32_t)((uint64_t)step >> 32);
-        call = 0; avail = 0; has_spare = 0; spare = T(0); status = 0;
+        call = 0; avail = 0; status = 0;
         b0 = b1 = b2 = b3 = 0;
     }
     __device__ __forceinline__ uint32_t u32()
@@ -277,23 +306,10 @@ struct Stream {
     }
     // uniform on (0,1)
     __device__ __forceinline__ T open();
-    __device__ __forceinline__ T normal()
-    {
-        if (has_spare) { has_spare = 0; return spare; }
-        for (int it = 0; it < 64; ++it) {
-            const T u = T(2) * open() - T(1);
-            const T v = T(2) * open() - T(1);
-            const T s = u * u + v * v;
-            if (s < T(1) && s > T(0)) {
-                const T f = Tr<T>::sqrt_((T(-2) * tm_log(s)) / s);
-                spare = v * f; has_spare = 1;
-                return u * f;
-            }
-        }
-        status |= TM_STATUS_CAP_BIT;
-        return T(0);
-    }
+    template <class Tab>
+    __device__ __forceinline__ T normal(const Tab& tb);
 };
+
 template <> __device__ __forceinline__ double Stream<double>::open()
 {
     const uint32_t w1 = u32();
@@ -305,6 +321,58 @@ template <> __device__ __forceinline__ float Stream<float>::open()
 {
     const uint32_t w = u32();
     return ((float)(w >> 8) + 0.5f) * 0x1p-24f;
+}
+
+// Tables every sampler reads, staged in shared memory by the kernel:
+// rcp[n] = 1/n (n <= 200) and the ziggurat (K: thresholds, W: widths, F: f(x_i)).
+constexpr int kRcpTable = 201;
+template <typename T>
+struct SmemTab {
+    T rcp[kRcpTable];
+    T zw[kZigN];
+    T zf[kZigN + 1];
+    uint32_t zk[kZigN];
+    __device__ __forceinline__ void fill()
+    {
+        for (int i = threadIdx.x; i < kRcpTable; i += blockDim.x) rcp[i] = (i == 0) ? T(0) : T(1) / (T)i;
+        for (int i = threadIdx.x; i < kZigN; i += blockDim.x) {
+            zw[i] = (T)kZigW[i];
+            zk[i] = kZigK[i];
+        }
+        for (int i = threadIdx.x; i <= kZigN; i += blockDim.x) zf[i] = (T)kZigF[i];
+    }
+};
+
+// standard normal by the ziggurat: one 32-bit word per attempt (layer index
+// from the low 7 bits, signed value from the top 25), wedge test or
+// Marsaglia's tail method when the fast test fails.
+template <typename T>
+template <class Tab>
+__device__ __forceinline__ T Stream<T>::normal(const Tab& tb)
+{
+    for (int it = 0; it < 64; ++it) {
+        const uint32_t w = u32();
+        const int iz = (int)(w & 127u);
+        const int32_t hz = (int32_t)(w >> 7) - (int32_t)(1 << 24);
+        const uint32_t az = (uint32_t)(hz < 0 ? -hz : hz);
+        const T x = (T)hz * tb.zw[iz];
+        if (az < tb.zk[iz]) return x;
+        if (iz == 0) {
+            for (int jt = 0; jt < 64; ++jt) {
+                const T xt = -tm_log_pos(open()) * T(1.0 / kZigR);
+                const T yt = -tm_log_pos(open());
+                if (yt + yt >= xt * xt) {
+                    const T r = T(kZigR) + xt;
+                    return hz < 0 ? -r : r;
+                }
+            }
+            break;
+        }
+        const T fb = tb.zf[iz], ft = tb.zf[iz + 1];
+        if (fb + open() * (ft - fb) < tm_exp(T(-0.5) * (x * x))) return x;
+    }
+    status |= TM_STATUS_CAP_BIT;
+    return T(0);
 }
 
 // log k!, k < 16
@@ -331,31 +399,31 @@ __device__ __forceinline__ double logfact_small(int k)
 
 // ---------------------------------------------------------------- samplers
 template <typename T>
-__device__ __forceinline__ T poisson_exact(Stream<T>& g, T m)
+__device__ __forceinline__ T poisson_exact(Stream<T>& g, T m, const SmemTab<T>& tb)
 {
     if (!(m > T(0))) return T(0);
-    if (m < T(10)) {
+    if (m < T(32)) {
         const uint32_t w = g.u32();
         const T u = (T)w * T(0x1p-32);
         T p = tm_exp(-m);
-        T q = tm_negexpm1(m);
+        T q = (m < T(0.25)) ? tm_negexpm1(m) : T(1) - p;  // tm_negexpm1's own split
         T n = T(0);
         int it = 0;
         while (u < q && it < 200) {
-            n = n + T(1);
-            p = (p * m) / n;
-            q = q - p;
             ++it;
+            n = n + T(1);
+            p = (p * m) * tb.rcp[it];
+            q = q - p;
         }
         return n;
     }
     const T slam = Tr<T>::sqrt_(m);
-    const T loglam = tm_log(m);
+    const T loglam = tm_log_pos(m);
     const T b = T(0.931) + T(2.53) * slam;
     const T a = T(-0.059) + T(0.02483) * b;
     const T invalpha = T(1.1239) + T(1.1328) / (b - T(3.4));
     const T vr = T(0.9277) - T(3.6224) / (b - T(2));
-    const T loginvalpha = tm_log(invalpha);
+    const T loginvalpha = tm_log_pos(invalpha);
     for (int it = 0; it < 64; ++it) {
         const T U = g.open() - T(0.5);
         const T V = g.open();
@@ -363,7 +431,7 @@ __device__ __forceinline__ T poisson_exact(Stream<T>& g, T m)
         const T k = Tr<T>::floor_((T(2) * a / us + b) * U + m + T(0.43));
         if (us >= T(0.07) && V <= vr) return k;
         if (k < T(0) || (us < T(0.013) && V > us)) continue;
-        const T lhs = (tm_log(V) + loginvalpha) - tm_log(a / (us * us) + b);
+        const T lhs = (tm_log_pos(V) + loginvalpha) - tm_log_pos(a / (us * us) + b);
         T rhs;
         if (k < T(16)) {
             rhs = (k * loglam - m) - (T)logfact_small((int)k);
@@ -373,7 +441,7 @@ __device__ __forceinline__ T poisson_exact(Stream<T>& g, T m)
             const T iz = T(1) / z;
             const T iz2 = iz * iz;
             const T corr = iz * (T(1.0 / 12.0) - iz2 * (T(1.0 / 360.0) - iz2 * T(1.0 / 1260.0)));
-            rhs = ((d - k * tm_log1p(d / m)) - T(0.5) * tm_log(z)) - (T(0x1.d67f1c864beb4p-1) + corr);
+            rhs = ((d - k * tm_log1p(d / m)) - T(0.5) * tm_log_pos(z)) - (T(0x1.d67f1c864beb4p-1) + corr);
         }
         if (lhs <= rhs) return k;
     }
@@ -382,7 +450,7 @@ __device__ __forceinline__ T poisson_exact(Stream<T>& g, T m)
 }
 
 template <typename T>
-__device__ __forceinline__ T gamma_mt(Stream<T>& g, T k)
+__device__ __forceinline__ T gamma_mt(Stream<T>& g, T k, const SmemTab<T>& tb)
 {
     if (!(k > T(0))) return T(0);
     const T kk = (k < T(1)) ? k + T(1) : k;
@@ -394,7 +462,7 @@ __device__ __forceinline__ T gamma_mt(Stream<T>& g, T k)
         T x = T(0), v = T(0);
         bool ok = false;
         for (int jt = 0; jt < 64; ++jt) {
-            x = g.normal();
+            x = g.normal(tb);
             v = T(1) + c * x;
             if (v > T(0)) { ok = true; break; }
         }
@@ -403,46 +471,99 @@ __device__ __forceinline__ T gamma_mt(Stream<T>& g, T k)
         const T u = g.open();
         const T x2 = x * x;
         if (u < T(1) - T(0.0331) * (x2 * x2)) { res = d * v; done = true; break; }
-        if (tm_log(u) < T(0.5) * x2 + d * ((T(1) - v) + tm_log(v))) { res = d * v; done = true; break; }
+        if (tm_log_pos(u) < T(0.5) * x2 + d * ((T(1) - v) + tm_log(v))) { res = d * v; done = true; break; }
     }
     if (!done) g.status |= TM_STATUS_CAP_BIT;
     if (k < T(1)) {
         const T u = g.open();
-        res = res * tm_exp(tm_log(u) / k);
+        res = res * tm_exp(tm_log_pos(u) / k);
     }
     return res;
 }
 
 // sampler: 0 exact, 1 Gaussian above 100 (multiSPDP.cpp:2915-2943)
 template <typename T>
-__device__ __forceinline__ T poisson_draw(Stream<T>& g, T m, int sampler)
+__device__ __forceinline__ T poisson_draw(Stream<T>& g, T m, int sampler, const SmemTab<T>& tb)
 {
     if (!(m > T(0))) return T(0);
     if (sampler == 1 && m > T(100)) {
-        const T z = g.normal();
+        const T z = g.normal(tb);
         return Tr<T>::trunc_(z * Tr<T>::sqrt_(m) + m);
     }
-    return poisson_exact(g, m);
+    return poisson_exact(g, m, tb);
 }
 
 template <typename T>
-__device__ __forceinline__ T gamma_draw(Stream<T>& g, T k, int sampler)
+__device__ __forceinline__ T gamma_draw(Stream<T>& g, T k, int sampler, const SmemTab<T>& tb)
 {
     if (sampler == 1 && k > T(100)) {
-        const T z = g.normal();
+        const T z = g.normal(tb);
         return z * Tr<T>::sqrt_(k) + k;
     }
-    return gamma_mt(g, k);
+    return gamma_mt(g, k, tb);
 }
 
 // rho* = Gamma(mu1 + Poisson(m)) / lambda  (stochasticSPDP.cpp:1053-1059)
 template <typename T>
-__device__ __forceinline__ T dornic_draw(Stream<T>& g, T m, T mu1, T inv_lambda, int sampler)
+__device__ __forceinline__ T dornic_draw(Stream<T>& g, T m, T mu1, T inv_lambda, int sampler,
+                                        const SmemTab<T>& tb)
 {
-    const T n = poisson_draw(g, m, sampler);
+    const T n = poisson_draw(g, m, sampler, tb);
     const T k = mu1 + n;
-    const T gv = gamma_draw(g, k, sampler);
+    const T gv = gamma_draw(g, k, sampler, tb);
     return gv * inv_lambda;
+}
+
+// Straight-line draw for the common case (FP32): one Philox block of four
+// words, Poisson by inversion finishing within kFastInv steps, shape >= 1, a
+// ziggurat normal accepted by its fast test and one Marsaglia-Tsang attempt
+// accepted by the squeeze.  Every step consumes the counter stream exactly as
+// dornic_draw does, so when it returns without deferring the value equals
+// dornic_draw's bit for bit; otherwise (*deferred) the caller recomputes the
+// site with dornic_draw.
+constexpr int kFastInv = 24;
+
+__device__ __forceinline__ float dornic_draw_fast(uint64_t seed, uint32_t site, int64_t step, float m, float mu1,
+                                                  float inv_lambda, int sampler, const SmemTab<float>& tb,
+                                                  bool& deferred)
+{
+    deferred = false;
+    const U4 r = philox4x32_10(site, (uint32_t)(uint64_t)step, 0u, (uint32_t)((uint64_t)step >> 32),
+                               (uint32_t)seed, (uint32_t)(seed >> 32));
+    float n = 0.0f;
+    const bool draw = m > 0.0f;
+    if (draw) {
+        if (!(m < 32.0f)) { deferred = true; return 0.0f; }
+        const float u = (float)r.x * 0x1p-32f;
+        float p = tm_exp(-m);
+        float q = (m < 0.25f) ? tm_negexpm1(m) : 1.0f - p;
+        int it = 0;
+        while (u < q && it < kFastInv) {
+            ++it;
+            n = n + 1.0f;
+            p = (p * m) * tb.rcp[it];
+            q = q - p;
+        }
+        if (u < q) { deferred = true; return 0.0f; }
+    }
+    const float k = mu1 + n;
+    if (!(k > 0.0f)) return 0.0f;  // Gamma(0) = 0, no draw
+    if (k < 1.0f || (sampler == 1 && k > 100.0f)) { deferred = true; return 0.0f; }
+    const uint32_t wz = draw ? r.y : r.x, wu = draw ? r.z : r.y;
+    const float d = k - (float)(1.0 / 3.0);
+    const float c = 1.0f / sqrtf(9.0f * d);
+    const int iz = (int)(wz & 127u);
+    const int32_t hz = (int32_t)(wz >> 7) - (int32_t)(1 << 24);
+    const uint32_t az = (uint32_t)(hz < 0 ? -hz : hz);
+    if (!(az < tb.zk[iz])) { deferred = true; return 0.0f; }
+    const float x = (float)hz * tb.zw[iz];
+    float v = 1.0f + c * x;
+    if (!(v > 0.0f)) { deferred = true; return 0.0f; }
+    v = (v * v) * v;
+    const float u = ((float)(wu >> 8) + 0.5f) * 0x1p-24f;
+    const float x2 = x * x;
+    if (!(u < 1.0f - 0.0331f * (x2 * x2))) { deferred = true; return 0.0f; }
+    return (d * v) * inv_lambda;
 }
 
 template <typename T>

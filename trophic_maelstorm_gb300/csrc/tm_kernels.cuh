@@ -36,6 +36,7 @@ struct DornicArgs {
     T dcoef, two_s2, b, c, dt, dt2, dt6, clo, ceps;
     int sampler;                   // 0 exact, 1 Gaussian above 100, 2 mean (noise off)
     int cubic;
+    int rows_cap;                  // rows of the largest task (<= kMaxRowsPerTask)
 };
 
 template <typename T>
@@ -75,6 +76,7 @@ template <typename T>
 cudaError_t launch_det_final(const T* x0, const T* k1, const T* k2, const T* k3, const T* k4, T* out, long long n,
                              T dt, T dt6, int rk4, cudaStream_t s);
 
+constexpr int kMaxRowsPerTask = 16;
 constexpr int RK_TX = 32, RK_TY = 16, RK_H = 4;
 constexpr int RK_RX = RK_TX + 2 * RK_H, RK_RY = RK_TY + 2 * RK_H, RK_RN = RK_RX * RK_RY;
 constexpr int RK_THREADS = 256;

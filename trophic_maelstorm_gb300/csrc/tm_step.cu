@@ -1,10 +1,13 @@
 // tm_step.cu -- the fused Dornic step for sm_103a.
 //
-// One warp owns a strip of 32 columns x R rows of one instance ("task") and
-// walks down it with a three-row register window (north, centre, south);
-// east/west neighbours come from warp shuffles, the two strip-edge columns
-// from global memory.  Each lattice value is read from HBM once per step and
-// written once (8 B per site-update in FP32).  Per site it fuses:
+// One warp owns a strip of 32 columns x R rows (R <= 16) of one instance
+// ("task") and walks down it with a three-row register window (north,
+// centre, south); east/west neighbours come from warp shuffles, the two
+// strip-edge columns from global memory.  Each lattice value is read from HBM
+// once per step and written once (8 B per site-update in FP32).  Sites that
+// need a random draw are compacted into a per-warp queue in shared memory so
+// that every lane of the sampler loop works on a live site: absorbing sites
+// never occupy a sampler lane.  Per site it fuses:
 //   alpha_i  = (D/dx^2) * sum of the 4 neighbours       stochasticSPDP.cpp:1037-1038
 //   skip     if alpha_i == 0 and rho_i == 0             :1049-1052
 //   rho*     = Gamma(2 alpha_i/sigma^2 + Poisson(lambda e^{beta dt} rho_i)) / lambda   :1053-1059
@@ -29,10 +32,32 @@ __device__ __forceinline__ T rem_f(T x, T b, T c, int cubic)
     return f;
 }
 
-template <typename T, int REM>
-__global__ void __launch_bounds__(256) dornic_step_kernel(const DornicArgs<T> A)
+// Per-warp shared scratch for one task of up to rows_cap rows: the Dornic draw
+// of every site (res), and the queue of live sites (index, Poisson mean, shape).
+constexpr int kWarps = 8;
+
+template <typename T>
+__host__ __device__ __forceinline__ size_t warp_scratch_bytes(int rows_cap)
 {
+    return (size_t)rows_cap * 32 * (3 * sizeof(T) + 2 * sizeof(unsigned short));
+}
+
+template <typename T, int REM>
+__global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_kernel(const DornicArgs<T> A)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ SmemTab<T> tab;
+    tab.fill();
+    __syncthreads();
+    const int cap = A.rows_cap * 32;
+    unsigned char* wbase = smem_raw + (threadIdx.x >> 5) * warp_scratch_bytes<T>(A.rows_cap);
+    T* const Wres = reinterpret_cast<T*>(wbase);
+    T* const Wqm = Wres + cap;
+    T* const Wqmu = Wqm + cap;
+    unsigned short* const Wqi = reinterpret_cast<unsigned short*>(Wqmu + cap);
+    unsigned short* const Wdef = Wqi + cap;
     const int lane = threadIdx.x & 31;
+    const unsigned lt_mask = (1u << lane) - 1u;
     const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int nw = (int)((gridDim.x * blockDim.x) >> 5);
     const long long step = (A.step_base ? *A.step_base : 0LL) + A.step_off;
@@ -45,7 +70,6 @@ __global__ void __launch_bounds__(256) dornic_step_kernel(const DornicArgs<T> A)
         T* __restrict__ dst = A.out + A.it.off[k];
         const Dc4 cs = A.it.consts[k];
         const T pm = (T)cs.x, inv_lambda = (T)cs.y, a1 = (T)cs.z, a2 = (T)cs.w;
-        const unsigned long long seed = A.it.seed[k];
         const int x0 = tk.y, y0 = tk.z, rows = tk.w;
         const int w = min(32, L - x0);
         const int x = x0 + lane;
@@ -53,9 +77,11 @@ __global__ void __launch_bounds__(256) dornic_step_kernel(const DornicArgs<T> A)
         const int xw = (x0 == 0) ? L - 1 : x0 - 1;
         const int xe = (x0 + w == L) ? 0 : x0 + w;
         const int yn = (y0 == 0) ? L - 1 : y0 - 1;
+        // pass 1: stream the rows, form alpha_i, resolve absorbing sites and the
+        // noise-off mean directly, queue the live sites (row-major order)
         T north = act ? src[(long long)yn * L + x] : T(0);
         T cur = act ? src[(long long)y0 * L + x] : T(0);
-        unsigned st = 0;
+        int nq = 0;
         for (int r = 0; r < rows; ++r) {
             const int y = y0 + r;
             const int ys = (y == L - 1) ? 0 : y + 1;
@@ -64,20 +90,64 @@ __global__ void __launch_bounds__(256) dornic_step_kernel(const DornicArgs<T> A)
             T east = __shfl_down_sync(0xffffffffu, cur, 1);
             if (lane == 0) west = src[(long long)y * L + xw];
             if (lane == w - 1) east = src[(long long)y * L + xe];
-            if (act) {
-                const T nsum = ((north + south) + west) + east;
-                const T alpha = A.dcoef * nsum;
-                T rs;
-                if (alpha == T(0) && cur == T(0)) {
-                    rs = T(0);
-                } else if (A.sampler == 2) {
-                    rs = a1 * cur + a2 * alpha;
-                } else {
-                    Stream<T> g;
-                    g.init(seed, (uint32_t)(y * L + x), step);
-                    rs = dornic_draw(g, pm * cur, alpha * A.two_s2, inv_lambda, A.sampler);
-                    st |= g.status;
+            const T nsum = ((north + south) + west) + east;
+            const T alpha = A.dcoef * nsum;
+            const bool live = act && !(alpha == T(0) && cur == T(0)) && A.sampler != 2;
+            if (!live) Wres[r * 32 + lane] = (A.sampler == 2 && act) ? a1 * cur + a2 * alpha : T(0);
+            const unsigned bal = __ballot_sync(0xffffffffu, live);
+            if (live) {
+                const int pos = nq + __popc(bal & lt_mask);
+                Wqi[pos] = (unsigned short)(r * 32 + lane);
+                Wqm[pos] = pm * cur;
+                Wqmu[pos] = alpha * A.two_s2;
+            }
+            nq += __popc(bal);
+            north = cur;
+            cur = south;
+        }
+        __syncwarp();
+        // pass 2: every lane draws for queued sites until the queue is empty.  FP32
+        // takes the straight-line common case first and compacts the rest into a
+        // second queue drawn with the general sampler (same stream, same bits).
+        unsigned st = 0;
+        const unsigned long long seed = A.it.seed[k];
+        int ndef = 0;
+        if constexpr (sizeof(T) == 4) {
+            for (int base = 0; base < nq; base += 32) {
+                const int j = base + lane;
+                const bool has = j < nq;
+                bool deferred = false;
+                if (has) {
+                    const int li = Wqi[j];
+                    const int site = (y0 + (li >> 5)) * L + x0 + (li & 31);
+                    const float v = dornic_draw_fast(seed, (uint32_t)site, step, Wqm[j], Wqmu[j], inv_lambda,
+                                                     A.sampler, tab, deferred);
+                    if (!deferred) Wres[li] = v;
                 }
+                const unsigned bal = __ballot_sync(0xffffffffu, has && deferred);
+                if (has && deferred) Wdef[ndef + __popc(bal & lt_mask)] = (unsigned short)j;
+                ndef += __popc(bal);
+            }
+            __syncwarp();
+        } else {
+            for (int j = lane; j < nq; j += 32) Wdef[j] = (unsigned short)j;
+            ndef = nq;
+            __syncwarp();
+        }
+        for (int jj = lane; jj < ndef; jj += 32) {
+            const int j = Wdef[jj];
+            const int li = Wqi[j];
+            const int site = (y0 + (li >> 5)) * L + x0 + (li & 31);
+            Stream<T> g;
+            g.init(seed, (uint32_t)site, step);
+            Wres[li] = dornic_draw(g, Wqm[j], Wqmu[j], inv_lambda, A.sampler, tab);
+            st |= g.status;
+        }
+        __syncwarp();
+        // pass 3: remainder, clamp, store
+        if (act) {
+            for (int r = 0; r < rows; ++r) {
+                const T rs = Wres[r * 32 + lane];
                 T res;
                 if (REM == 0) {
                     res = rs / (T(1) + (A.b * rs) * A.dt);
@@ -94,11 +164,10 @@ __global__ void __launch_bounds__(256) dornic_step_kernel(const DornicArgs<T> A)
                     if (res < A.ceps && res >= A.clo) res = T(0);
                     st |= value_status(res);
                 }
-                dst[(long long)y * L + x] = res;
+                dst[(long long)(y0 + r) * L + x] = res;
             }
-            north = cur;
-            cur = south;
         }
+        __syncwarp();
         if (st) atomicOr(A.it.status + k, st);
     }
 }
@@ -107,9 +176,21 @@ template <typename T>
 cudaError_t launch_dornic(const DornicArgs<T>& a, int rem, int grid, int block, cudaStream_t s)
 {
     if (a.n_tasks <= 0) return cudaSuccess;
-    if (rem == 0) dornic_step_kernel<T, 0><<<grid, block, 0, s>>>(a);
-    else if (rem == 1) dornic_step_kernel<T, 1><<<grid, block, 0, s>>>(a);
-    else dornic_step_kernel<T, 2><<<grid, block, 0, s>>>(a);
+    if (block != 32 * kWarps || a.rows_cap < 1 || a.rows_cap > kMaxRowsPerTask) return cudaErrorInvalidValue;
+    const size_t smem = warp_scratch_bytes<T>(a.rows_cap) * kWarps;
+    static bool attr_set[3] = {false, false, false};
+    const int full = (int)(warp_scratch_bytes<T>(kMaxRowsPerTask) * kWarps);
+    cudaError_t e = cudaSuccess;
+    if (!attr_set[rem]) {
+        if (rem == 0) e = cudaFuncSetAttribute(dornic_step_kernel<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, full);
+        else if (rem == 1) e = cudaFuncSetAttribute(dornic_step_kernel<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, full);
+        else e = cudaFuncSetAttribute(dornic_step_kernel<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, full);
+        if (e != cudaSuccess) return e;
+        attr_set[rem] = true;
+    }
+    if (rem == 0) dornic_step_kernel<T, 0><<<grid, block, smem, s>>>(a);
+    else if (rem == 1) dornic_step_kernel<T, 1><<<grid, block, smem, s>>>(a);
+    else dornic_step_kernel<T, 2><<<grid, block, smem, s>>>(a);
     return cudaGetLastError();
 }
 template cudaError_t launch_dornic<float>(const DornicArgs<float>&, int, int, int, cudaStream_t);
