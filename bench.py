@@ -135,13 +135,22 @@ def barrier(world):
 
 
 def max_over_ranks(v, world):
+    """Slowest rank's time (the job's time): all-reduce MAX over the process group
+    (NCCL on GPU ranks, gloo on CPU)."""
     if world <= 1:
         return v
     import torch
     import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def job_throughput(units_per_rank, seconds_per_rank, world):
+    """Whole-job throughput of independent replicas: every rank's units over the
+    slowest rank's time (weak scaling)."""
+    return units_per_rank * world / max_over_ranks(seconds_per_rank, world)
 
 
 # ------------------------------------------------------------------ CPU baseline
@@ -284,6 +293,36 @@ def late_regime(ctx, tmg, torch, args, burn=600, steps=10):
             "hbm_frac": BYTES_PER_SITE_FP32 * sites / (ms * 1e-3) / 1e9 / peaks()[0]}
 
 
+def rietkerk_4096(ctx, tmg, torch, args, steps=10, L=4096, precision=None):
+    """The single large Rietkerk instance: 4096^2 three-field lattice, R = 0.9,
+    sigma = 0.5, RK4 dt = 1e-3 (Dornic draw on P + fused RK4 of the remainder).
+    Algorithmic traffic 24 B/site FP32 (read and write P, W, O once)."""
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    precision = tmg.TM_FP32 if precision is None else precision
+    inst = tmg.instances([L], [2024], 0.9)
+    b = tmg.Batch(ctx, tmg.rietkerk_model(), inst, precision)
+    rng = np.random.default_rng(3)
+    dtype = np.float32 if precision == tmg.TM_FP32 else np.float64
+    f0 = np.stack([rng.uniform(0, 1, (L, L)), np.full((L, L), 0.5), np.full((L, L), 1.0)]).astype(dtype)
+    b.upload([f0])
+    b.enqueue_steps(3)
+    ctx.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        for _ in range(steps):
+            b.enqueue_steps(1)
+        e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    b.close()
+    sites = L * L
+    bps = (24 if precision == tmg.TM_FP32 else 48) * sites / (ms * 1e-3) / 1e9
+    return {"L": L, "precision": "f32" if precision == tmg.TM_FP32 else "f64", "ms_per_step": ms,
+            "site_updates_per_s": sites / (ms * 1e-3), "achieved_gbs_alg": bps, "hbm_frac": bps / peaks()[0],
+            "kernels_per_step": 2}
+
+
 def run_ours(args):
     import torch
     import trophic_maelstorm_gb300 as tmg
@@ -362,6 +401,7 @@ def run_ours(args):
     if not args.no_extras:
         extras["plain_fp64_single_instance"] = plain_fp64(ctx, tmg, torch, args)
         extras["late_regime"] = late_regime(ctx, tmg, torch, args)
+        extras["rietkerk_4096"] = rietkerk_4096(ctx, tmg, torch, args)
 
     hbm, peak_kind = peaks()
     avg_launch_s = statistics.mean(per) * 1e-3

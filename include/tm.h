@@ -215,6 +215,21 @@ int tm_run_rietkerk(tm_ctx* ctx, const tm_rietkerk_model* model, const tm_instan
 int tm_observe_noalloc(const void* dev_fields, int precision, const int32_t* L, const int64_t* offsets,
                        int n_inst, double* dev_out, void* stream);
 
+/* -- pattern wavelength --------------------------------------------------
+ * Radially averaged power spectrum of one L x L lattice in device memory, with
+ * the semantics of the reference's estimator gen_FFT_PowerSpectra
+ * (simulations/Utilities/glow_up.py:752-827): divide by the maximum (if
+ * non-zero), |FFT2|^2 in double precision, mean over annuli of width binwidth
+ * starting at 1 - binwidth/2, times the annulus area; empty bins are 0 (the
+ * reference turns them into NaN).  kvals/power receive *n_bins values
+ * (TM_ERR_INVALID if more than max_bins).  The pattern wavelength is
+ * L / kvals[argmax power].  Synchronises `stream`. */
+int tm_power_spectrum_device(const void* dev_field, int precision, int L, double binwidth, void* stream,
+                             double* kvals, double* power, int max_bins, int* n_bins);
+/* The same for field `field` of instance k of a batch's current state. */
+int tm_batch_power_spectrum(tm_batch* b, int k, int field, double binwidth, double* kvals, double* power,
+                            int max_bins, int* n_bins);
+
 /* Packed-layout geometry without a batch (for callers that pack host buffers
  * before creating one): offsets[k] and the total, for nf fields per instance. */
 int64_t tm_layout(const tm_instance* inst, int n_inst, int nf, int64_t* offsets, int64_t* field_strides);

@@ -11,6 +11,8 @@ Fixtures
 ref_pins.npz       deterministic outputs of the reference's stage functions
                    (noise-off Rietkerk RK4, stochastic-remainder RK4s, the
                    4th-order noise-off DP RK4, logarithm10_time_bins).
+ref_csv.npz        files written by the reference's own save_frame / save_prelimframe
+                   (multiSPDP.cpp:1493-1643), byte for byte.
 ref_dp_ensemble.npz  per-replicate trajectories of percolationDornic_2D
                    (stochasticSPDP.cpp:940), one replicate per call.  The
                    reference seeds std::mt19937_64 from std::random_device, so
@@ -51,6 +53,9 @@ def load():
     r.ref_rk_det_steps.argtypes = [dp, C.c_int, C.c_int] + [C.c_double] * 14
     r.ref_rk_stoch_remainder.argtypes = [dp, C.c_int] + [C.c_double] * 12
     libs["multisp"].ref_ms_rk4_remainder.argtypes = [dp, C.c_int, C.c_double, C.c_double, C.c_double]
+    cs = C.c_char_p
+    libs["multisp"].ref_save_frame.argtypes = [dp, C.c_int, cs, cs, C.c_double, C.c_int, cs]
+    libs["multisp"].ref_save_prelim.argtypes = [dp, C.c_int, C.c_int, cs, cs, C.c_double, C.c_int, cs]
     return libs
 
 
@@ -122,10 +127,38 @@ def ensemble(libs, rng, L, a, tm, n_rep, b=2.0, D=1.0, sigma=1.0, dt=0.1, dx=1.0
                 meta=np.array([L, a, b, D, sigma, dt, dx]))
 
 
+def csv_writers(libs, rng):
+    """Files written by the reference's save_frame / save_prelimframe, including the
+    collision-safe renumbering when a file of the same name exists."""
+    import tempfile
+    out = {}
+    with tempfile.TemporaryDirectory() as d:
+        g = 6
+        rho = np.concatenate([rng.uniform(0, 2, g * g - 4), [0.0, 1e-30, 123456.789, 0.1]])
+        pat = "/FRAME_T_G_6_a_0.72_R_"
+        hdr = "a_c,  x,  P(x; t) \n"
+        for _ in range(3):  # R_0, then renumbered R_1, R_2
+            libs["multisp"].ref_save_frame(_p(rho), g, d.encode(), pat.encode(), 0.72, 0, hdr.encode())
+        for k in range(3):
+            out[f"frame_R_{k}"] = np.frombuffer(open(f"{d}{pat}{k}.csv", "rb").read(), np.uint8)
+        out["frame_in"] = rho
+        rows = np.stack([np.arange(7) * 0.5, rng.uniform(0, 1, 7), rng.uniform(0, 0.01, 7),
+                         rng.integers(0, 5, 7).astype(float), rng.integers(0, 36, 7).astype(float)], axis=1)
+        rows[3, 1] = 1.0 / 3.0
+        ppat = "/PRELIM_AGG_T_G_6_a_0.72_R_"
+        phdr = " a , r, L, t , <<P(x; t)>_x>_r, Var[<P(x; t)>_x]_r, # Surviving Runs P(x; t), # Active Sites P(x; t), \n"
+        libs["multisp"].ref_save_prelim(_p(np.ascontiguousarray(rows)), 7, g, d.encode(), ppat.encode(), 0.72, 4,
+                                        phdr.encode())
+        out["prelim_R_4"] = np.frombuffer(open(f"{d}{ppat}4.csv", "rb").read(), np.uint8)
+        out["prelim_in"] = rows
+    return out
+
+
 def main():
     libs = load()
     rng = np.random.default_rng(20261203)
     np.savez_compressed(os.path.join(HERE, "ref_pins.npz"), **pins(libs, rng))
+    np.savez_compressed(os.path.join(HERE, "ref_csv.npz"), **csv_writers(libs, np.random.default_rng(7)))
     ens = {}
     tm = [1.5, 2.0, 3.0, 5.0, 8.0, 10.0, 20.0, 50.0]
     for tag, L, a, n in (("crit", 8, 0.72, 1500), ("active", 8, 2.0, 800), ("site", 1, 0.72, 3000)):

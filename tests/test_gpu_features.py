@@ -1,0 +1,122 @@
+"""GPU tests of the rows next to the step: pattern wavelength (power spectrum),
+checkpoint/resume, the command-line sweep driver and its CSV outputs."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def tmg():
+    from trophic_maelstorm_gb300 import build
+    build.build()
+    import trophic_maelstorm_gb300 as m
+    return m
+
+
+@pytest.fixture(scope="module")
+def ctx(tmg):
+    return tmg.Context(0)
+
+
+def spectrum_numpy(img, binwidth=0.5):
+    """gen_FFT_PowerSpectra (glow_up.py:752-827) for one column, restated with numpy:
+    max-normalise, |fft2|^2, radial bins from 1 - w/2 with np.histogram, mean x area."""
+    L = img.shape[0]
+    img = img.astype(np.float64)
+    mx = img.max()
+    img = img / (mx if mx != 0.0 else 1.0)
+    kbins = np.arange(1 - binwidth / 2, L // 2 + 1, binwidth)
+    kvals = 0.5 * (kbins[1:] + kbins[:-1])
+    F = np.fft.fft2(img)
+    kf = np.fft.fftfreq(L) * L
+    kx, ky = np.meshgrid(kf, kf)
+    knrm = np.sqrt(kx ** 2 + ky ** 2).flatten()
+    amp = np.abs(F ** 2).flatten()
+    s, _ = np.histogram(knrm, bins=kbins, weights=amp)
+    c, _ = np.histogram(knrm, bins=kbins)
+    p = np.divide(s, c, out=np.zeros_like(s), where=c != 0)
+    p *= np.pi * (kbins[1:] ** 2 - kbins[:-1] ** 2)
+    return kvals, p
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32"])
+@pytest.mark.parametrize("L", [16, 33, 128])
+def test_power_spectrum_matches_reference_semantics(tmg, ctx, precision, L):
+    rng = np.random.default_rng(L)
+    y, x = np.mgrid[0:L, 0:L]
+    lam = L / 4.0
+    f = 1.0 + 0.5 * np.sin(2 * np.pi * x / lam) + 0.05 * rng.random((L, L))  # stripes, |k| = L/lam
+    f = np.stack([f, rng.random((L, L)), np.zeros((L, L))])
+    dtype = np.float64 if precision == 0 else np.float32
+    b = tmg.Batch(ctx, tmg.rietkerk_model(), tmg.instances([L], [0], 0.9), precision)
+    b.upload([f.astype(dtype)])
+    for field in range(3):
+        kv, pw = b.power_spectrum(0, field)
+        rk, rp = spectrum_numpy(f[field].astype(dtype))
+        np.testing.assert_allclose(kv, rk, rtol=0, atol=1e-12)
+        np.testing.assert_allclose(pw, rp, rtol=1e-9, atol=1e-9 * max(1.0, rp.max()))
+    kv, pw = b.power_spectrum(0, 0)
+    if L % 4 == 0:
+        assert tmg.pattern_wavelength(L, kv, pw) == pytest.approx(lam)
+    b.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32"])
+def test_checkpoint_resume_is_bit_exact(tmg, ctx, tmp_path, precision):
+    from trophic_maelstorm_gb300 import io
+    dtype = np.float64 if precision == 0 else np.float32
+    Ls = [32, 64]
+    inst = tmg.instances(Ls, [11, 12], 0.72)
+    rng = np.random.default_rng(0)
+    init = [(1 + rng.uniform(-0.01, 0.01, (L, L))).astype(dtype) for L in Ls]
+    full = tmg.Batch(ctx, tmg.dp_model(), inst, precision)
+    full.upload(init)
+    full.advance(80)
+    ref = full.download_packed()
+    half = tmg.Batch(ctx, tmg.dp_model(), inst, precision)
+    half.upload(init)
+    half.advance(45)
+    path = str(tmp_path / "ck.npz")
+    io.save_checkpoint(half, path)
+    half.close()
+    again = tmg.Batch(ctx, tmg.dp_model(), inst, precision)
+    assert io.load_checkpoint(again, path) == 45
+    again.advance(35)
+    assert np.array_equal(again.download_packed(), ref)
+    full.close()
+    again.close()
+
+
+def test_sweep_driver_matches_python_api(tmg, ctx, tmp_path):
+    exe = os.path.join(REPO, "trophic_maelstorm_gb300", "lib", "tm_sweep")
+    out = str(tmp_path / "sweep")
+    r = subprocess.run([exe, "0.1", "5", "16", "6", "0.7", "0.8", "2", "0", "T", "--seed", "100", "--out", out],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    stats = [f for f in os.listdir(out) if f.startswith("T_P_c_Delta")]
+    assert len(stats) == 1
+    with open(os.path.join(out, stats[0])) as fh:
+        head = fh.readline()
+        got = np.loadtxt(fh, delimiter=",", ndmin=2)
+    assert head.startswith(" a , L, t")
+    # the same sweep through the Python API: 2 a-values x 6 replicates, seeds 100 + index
+    t_meas = tmg.logarithm10_time_bins(5.0, 0.1)
+    rows = []
+    for ia, a in enumerate([0.7, 0.8]):
+        rr, _ = tmg.percolation_dornic_2d(t_meas, np.ones(256), 5.0, a, 2.0, 1.0, 1.0, 0.1, 1.0, 6, 16,
+                                          seed=100 + ia * 6, ctx=ctx)
+        rows.append(rr)
+    want = np.concatenate(rows)
+    assert got.shape == want.shape
+    np.testing.assert_allclose(got, want, rtol=2e-5, atol=1e-12)   # 6 printed digits
+    assert len(os.listdir(os.path.join(out, "TimeSeries"))) == 2
+    frames = sorted(f for f in os.listdir(out) if f.startswith("FRAME_"))
+    assert len(frames) == 2
+    from trophic_maelstorm_gb300 import io
+    fr = io.read_frame(os.path.join(out, frames[0]), 16)
+    assert fr.shape == (16, 16) and np.all(fr >= 0)

@@ -26,7 +26,7 @@ EXPORTS = (
     "tm_batch_step", "tm_batch_upload", "tm_batch_download", "tm_batch_upload_device",
     "tm_batch_download_device", "tm_batch_snapshot", "tm_batch_advance", "tm_batch_enqueue_steps",
     "tm_batch_set_launch", "tm_batch_get_launch", "tm_batch_autotune", "tm_run_dp", "tm_run_rietkerk",
-    "tm_layout", "tm_observe_noalloc",
+    "tm_layout", "tm_observe_noalloc", "tm_power_spectrum_device", "tm_batch_power_spectrum",
 )
 
 
@@ -99,6 +99,10 @@ def lib():
                                  C.c_int, dp, u32p, vp], C.c_int),
             "tm_layout": ([C.POINTER(Instance), C.c_int, C.c_int, i64p, i64p], i64),
             "tm_observe_noalloc": ([vp, C.c_int, C.POINTER(C.c_int32), i64p, C.c_int, vp, vp], C.c_int),
+            "tm_power_spectrum_device": ([vp, C.c_int, C.c_int, C.c_double, vp, dp, dp, C.c_int,
+                                          C.POINTER(C.c_int)], C.c_int),
+            "tm_batch_power_spectrum": ([vp, C.c_int, C.c_int, C.c_double, dp, dp, C.c_int, C.POINTER(C.c_int)],
+                                        C.c_int),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)

@@ -235,6 +235,19 @@ class Batch:
         T.check(T.lib().tm_batch_autotune(self._h, steps_per_trial), "tm_batch_autotune")
         return self.get_launch()
 
+    def power_spectrum(self, k, field=0, binwidth=0.5):
+        """Radially averaged power spectrum of instance k's field (glow_up.py:752-827
+        semantics); returns (kvals, power)."""
+        L = self.inst[k].L
+        cap = int(2 * L / binwidth) + 8
+        kv = np.zeros(cap)
+        pw = np.zeros(cap)
+        nb = C.c_int()
+        T.check(T.lib().tm_batch_power_spectrum(self._h, k, field, binwidth, kv.ctypes.data_as(C.POINTER(C.c_double)),
+                                                pw.ctypes.data_as(C.POINTER(C.c_double)), cap, C.byref(nb)),
+                "tm_batch_power_spectrum")
+        return kv[:nb.value], pw[:nb.value]
+
     def close(self):
         if self._h:
             T.lib().tm_batch_destroy(self._h)
@@ -245,6 +258,12 @@ class Batch:
             self.close()
         except Exception:  # noqa: BLE001
             pass
+
+
+def pattern_wavelength(L, kvals, power):
+    """Wavelength (lattice units) at the peak of a radial power spectrum: L / k_peak."""
+    p = np.where(np.isfinite(power), power, -np.inf)
+    return float(L) / float(kvals[int(np.argmax(p))])
 
 
 def run_dp(ctx, model, inst, init_packed, n_steps, meas_steps, precision):

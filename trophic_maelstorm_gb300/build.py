@@ -21,7 +21,8 @@ CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "lib")
 OBJ_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT_DIR, "libtm.so")
-SOURCES = ["tm_step.cu", "tm_rk4.cu", "tm_measure.cu", "tm_capi.cu", "tm_noalloc.cu"]
+SWEEP = os.path.join(OUT_DIR, "tm_sweep")
+SOURCES = ["tm_step.cu", "tm_rk4.cu", "tm_measure.cu", "tm_capi.cu", "tm_noalloc.cu", "tm_spectrum.cu"]
 HEADERS = ["tm_device.cuh", "tm_kernels.cuh", "tm_zig_table.cuh", os.path.join("..", "..", "include", "tm.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
@@ -68,10 +69,18 @@ def build(verbose: bool = False, force: bool = False) -> str:
         for _, log in results:
             sys.stderr.write(log)
     if force or _stale(LIB, objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-lcufft"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    # the command-line sweep driver (host C++ over the C ABI)
+    src = os.path.join(CSRC, "tm_sweep.cpp")
+    if force or _stale(SWEEP, [src, LIB]):
+        cmd = [nvcc(), "-std=c++17", "-O2", "-o", SWEEP, src, "-L" + OUT_DIR, "-ltm",
+               "-Xlinker", "-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"tm_sweep build failed:\n{r.stdout}\n{r.stderr}")
     return LIB
 
 

@@ -770,6 +770,26 @@ int tm_batch_autotune(tm_batch* b, int steps_per_trial)
     return tm_batch_set_launch(b, best_r, best_c);
 }
 
+int tm_batch_power_spectrum(tm_batch* b, int k, int field, double binwidth, double* kvals, double* power,
+                            int max_bins, int* n_bins)
+{
+    if (!b || k < 0 || k >= b->n_inst || field < 0 || field >= b->nf) return TM_ERR_INVALID;
+    TM_CUDA(cudaSetDevice(b->ctx->device));
+    int alive = 1;
+    if (b->model == 0) TM_CUDA(cudaMemcpy(&alive, b->d_alive + k, sizeof(int), cudaMemcpyDeviceToHost));
+    if (!alive) {  // an extinct instance is all zeros: no power at any k
+        const int L = b->inst[k].L;
+        int rc = tm_power_spectrum_device(b->buf[b->cur], b->precision, L, binwidth, b->ctx->stream, kvals, power,
+                                          max_bins, n_bins);
+        if (rc == TM_OK)
+            for (int i = 0; i < *n_bins; ++i) power[i] = 0.0;
+        return rc;
+    }
+    const char* base = (const char*)b->buf[b->cur] + (size_t)(b->off[k] + field * b->fstride[k]) * b->esize;
+    return tm_power_spectrum_device(base, b->precision, b->inst[k].L, binwidth, b->ctx->stream, kvals, power,
+                                    max_bins, n_bins);
+}
+
 static int run_common(tm_batch* b, const void* init, int64_t n_steps, const int64_t* meas, int n_meas, double* obs,
                       uint32_t* status, void* fin)
 {

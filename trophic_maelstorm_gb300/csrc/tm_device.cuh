@@ -532,6 +532,23 @@ __device__ __forceinline__ float dornic_draw_fast(uint64_t seed, uint32_t site, 
                                (uint32_t)seed, (uint32_t)(seed >> 32));
     float n = 0.0f;
     const bool draw = m > 0.0f;
+    if (sampler == 1 && m > 100.0f) {
+        // Gaussian approximations of both draws (multiSPDP.cpp:2922-2943): one
+        // ziggurat word each
+        const int i1 = (int)(r.x & 127u);
+        const int32_t h1 = (int32_t)(r.x >> 7) - (int32_t)(1 << 24);
+        const uint32_t a1 = (uint32_t)(h1 < 0 ? -h1 : h1);
+        if (!(a1 < tb.zk[i1])) { deferred = true; return 0.0f; }
+        const float z1 = (float)h1 * tb.zw[i1];
+        const float kk = mu1 + truncf(z1 * sqrtf(m) + m);
+        if (!(kk > 100.0f)) { deferred = true; return 0.0f; }
+        const int i2 = (int)(r.y & 127u);
+        const int32_t h2 = (int32_t)(r.y >> 7) - (int32_t)(1 << 24);
+        const uint32_t a2 = (uint32_t)(h2 < 0 ? -h2 : h2);
+        if (!(a2 < tb.zk[i2])) { deferred = true; return 0.0f; }
+        const float z2 = (float)h2 * tb.zw[i2];
+        return (z2 * sqrtf(kk) + kk) * inv_lambda;
+    }
     if (draw) {
         if (!(m < 32.0f)) { deferred = true; return 0.0f; }
         const float u = (float)r.x * 0x1p-32f;

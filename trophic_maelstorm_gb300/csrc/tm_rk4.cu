@@ -62,16 +62,27 @@ __global__ void __launch_bounds__(RK_THREADS) rk4_tile_kernel(const RK4Args<T> A
                         const T Pc = S[0][c], Wc = S[1][c], Oc = S[2][c];
                         const T upt_num = (A.gmax * Wc) * Pc;
                         const T wk = Wc + A.k1;
-                        const T infil = ((A.alpha * (Pc + A.k2W0)) / (Pc + A.k2)) * Oc;
+                        T infil, fP, upt;
+                        if constexpr (sizeof(T) == 8) {
+                            // the reference's own expressions
+                            infil = ((A.alpha * (Pc + A.k2W0)) / (Pc + A.k2)) * Oc;
+                            fP = ((A.cgmax * Wc) * Pc) / wk;
+                            upt = upt_num / wk;
+                        } else {
+                            // FP32: two reciprocals instead of three divisions
+                            const T iwk = T(1) / wk;
+                            infil = ((A.alpha * (Pc + A.k2W0)) * (T(1) / (Pc + A.k2))) * Oc;
+                            fP = ((A.cgmax * Wc) * Pc) * iwk;
+                            upt = upt_num * iwk;
+                        }
                         const T lapW = (((S[1][cn] + S[1][cs]) + S[1][cw]) + S[1][ce]) - T(4) * Wc;
                         const T lapO = (((S[2][cn] + S[2][cs]) + S[2][cw]) + S[2][ce]) - T(4) * Oc;
-                        T fP = ((A.cgmax * Wc) * Pc) / wk;
                         if (DET) {
                             const T lapP = (((S[0][cn] + S[0][cs]) + S[0][cw]) + S[0][ce]) - T(4) * Pc;
                             fP = (fP - A.d * Pc) + A.DPx * lapP;
                         }
                         kv[j][0] = fP;
-                        kv[j][1] = ((infil - upt_num / wk) - A.rW * Wc) + A.DWx * lapW;
+                        kv[j][1] = ((infil - upt) - A.rW * Wc) + A.DWx * lapW;
                         kv[j][2] = (R - infil) + A.DOx * lapO;
                     }
                     if (s == 0) {
