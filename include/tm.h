@@ -174,6 +174,16 @@ int tm_batch_set_launch(tm_batch* b, int rows_per_task, int ctas_per_sm);
 int tm_batch_get_launch(const tm_batch* b, int* rows_per_task, int* ctas_per_sm);
 int tm_batch_autotune(tm_batch* b, int steps_per_trial);
 
+/* Per-site loss coefficient b_v for a DP batch (host, packed like the state):
+ * the remainder uses b_v[i] in place of tm_dp_model.b -- the termite-mound
+ * field of sde_RFT_2D_improved_Euler_w_mounds_RT_RK4_SNAPSHOTS_DEF.f:196-428,
+ * 564-574.  NULL restores the uniform b. */
+int tm_batch_set_site_coeff(tm_batch* b, const void* host_coeff);
+
+/* Kadanoff block means of field `field` of instance k (sde_RFT...DEF.f:474-516):
+ * out[(by * (L/box) + bx)] = mean over the box x box block; L % box must be 0. */
+int tm_batch_box_means(tm_batch* b, int k, int field, int box, double* out);
+
 /* -- one-shot calls: host buffers in, host results out -------------------- */
 /* The whole percolationDornic_2D-style job for a batch: upload init_fields,
  * advance n_steps with measurements, return obs/status and (optionally) the

@@ -65,6 +65,8 @@ def lib():
             getattr(L, f"tmo_sample_normal_{nm}").argtypes = [C.c_uint64, C.c_int64, C.c_int64, ptr]
             getattr(L, f"tmo_sample_dornic_{nm}").argtypes = [t, t, t, C.c_uint64, C.c_int64, C.c_int, C.c_int64, ptr, u32p]
             getattr(L, f"tmo_dp_step_{nm}").argtypes = [C.POINTER(DPParams), C.c_int, C.c_uint64, C.c_int64, ptr, ptr, u32p]
+            getattr(L, f"tmo_dp_step_sb_{nm}").argtypes = [C.POINTER(DPParams), C.c_int, C.c_uint64, C.c_int64, ptr, ptr,
+                                                           u32p, ptr]
             getattr(L, f"tmo_rk_step_{nm}").argtypes = [C.POINTER(RKParams), C.c_int, C.c_uint64, C.c_int64, ptr, ptr, u32p]
             getattr(L, f"tmo_rk_det_step_{nm}").argtypes = [C.POINTER(RKParams), C.c_int, ptr, ptr]
             getattr(L, f"tmo_dp_det_step_{nm}").argtypes = [C.c_double] * 6 + [C.c_int, C.c_int, C.c_int, ptr, ptr]
@@ -153,6 +155,16 @@ def dp_step(p, rho, seed, step):
     out = np.empty_like(rho)
     st = np.zeros(1, np.uint32)
     getattr(lib(), f"tmo_dp_step_{_sfx(rho.dtype)}")(C.byref(p), L, seed, step, _ptr(rho), _ptr(out), _ptr(st))
+    return out, int(st[0])
+
+
+def dp_step_sb(p, rho, seed, step, site_b):
+    rho = np.ascontiguousarray(rho)
+    sb = np.ascontiguousarray(site_b, dtype=rho.dtype)
+    out = np.empty_like(rho)
+    st = np.zeros(1, np.uint32)
+    getattr(lib(), f"tmo_dp_step_sb_{_sfx(rho.dtype)}")(C.byref(p), rho.shape[0], seed, step, _ptr(rho), _ptr(out),
+                                                          _ptr(st), _ptr(sb))
     return out, int(st[0])
 
 

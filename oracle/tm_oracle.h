@@ -102,6 +102,11 @@ int tmo_dp_step_f64(const tmo_dp_params* p, int L, uint64_t seed, int64_t step,
                     const double* in, double* out, uint32_t* status);
 int tmo_dp_step_f32(const tmo_dp_params* p, int L, uint64_t seed, int64_t step,
                     const float* in, float* out, uint32_t* status);
+/* the same with a per-site loss coefficient b_v (NULL: p->b everywhere) */
+int tmo_dp_step_sb_f64(const tmo_dp_params* p, int L, uint64_t seed, int64_t step,
+                       const double* in, double* out, uint32_t* status, const double* site_b);
+int tmo_dp_step_sb_f32(const tmo_dp_params* p, int L, uint64_t seed, int64_t step,
+                       const float* in, float* out, uint32_t* status, const float* site_b);
 int tmo_rk_step_f64(const tmo_rk_params* p, int L, uint64_t seed, int64_t step,
                     const double* in /* [P|W|O] 3*L*L */, double* out, uint32_t* status);
 int tmo_rk_step_f32(const tmo_rk_params* p, int L, uint64_t seed, int64_t step,

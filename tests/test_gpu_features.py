@@ -120,3 +120,48 @@ def test_sweep_driver_matches_python_api(tmg, ctx, tmp_path):
     from trophic_maelstorm_gb300 import io
     fr = io.read_frame(os.path.join(out, frames[0]), 16)
     assert fr.shape == (16, 16) and np.all(fr >= 0)
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32"])
+@pytest.mark.parametrize("remainder", [0, 1], ids=["euler", "rk4"])
+def test_site_coefficient_field_matches_oracle(tmg, oracle, ctx, precision, remainder):
+    """Per-site loss coefficient b_v (the Fortran RFT mound field) against the oracle, bit for bit."""
+    dtype = np.float64 if precision == 0 else np.float32
+    Ls = [24, 40]
+    rng = np.random.default_rng(5)
+    init = [(1 + rng.uniform(-0.01, 0.01, (L, L))).astype(dtype) for L in Ls]
+    bv = []
+    for L in Ls:
+        y, x = np.mgrid[0:L, 0:L]
+        mound = ((x - L / 2) ** 2 + (y - L / 3) ** 2) < (L / 5) ** 2
+        bv.append(np.where(mound, 0.5, 2.0).astype(dtype))
+    model = tmg.dp_model(b=2.0, c=0.3, remainder=remainder)
+    inst = tmg.instances(Ls, [1, 2], 0.72)
+    b = tmg.Batch(ctx, model, inst, precision)
+    b.set_site_coeff(bv)
+    b.upload(init)
+    b.advance(12)
+    fin = b.download()
+    for k, L in enumerate(Ls):
+        p = oracle.DPParams(0.72, 0.0, 2.0, 0.3, 1.0, 1.0, 0.1, 1.0, 0.0, 0.0, remainder, 0)
+        r = init[k]
+        for s in range(12):
+            r, _ = oracle.dp_step_sb(p, r, [1, 2][k], s, bv[k])
+        assert np.array_equal(fin[k], r)
+    b.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32"])
+def test_box_means(tmg, ctx, precision):
+    dtype = np.float64 if precision == 0 else np.float32
+    L = 64
+    rng = np.random.default_rng(1)
+    f = rng.random((3, L, L)).astype(dtype)
+    b = tmg.Batch(ctx, tmg.rietkerk_model(), tmg.instances([L], [0], 0.9), precision)
+    b.upload([f])
+    for field in range(3):
+        for box in (1, 4, 16, 64):
+            got = b.box_means(0, box, field)
+            want = f[field].astype(np.float64).reshape(L // box, box, L // box, box).mean(axis=(1, 3))
+            np.testing.assert_allclose(got, want, rtol=1e-12)
+    b.close()

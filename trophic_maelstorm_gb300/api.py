@@ -235,6 +235,24 @@ class Batch:
         T.check(T.lib().tm_batch_autotune(self._h, steps_per_trial), "tm_batch_autotune")
         return self.get_launch()
 
+    def set_site_coeff(self, coeff):
+        """Per-site loss coefficient b_v (list of (L, L) arrays or a packed buffer; None: uniform b)."""
+        if coeff is None:
+            T.check(T.lib().tm_batch_set_site_coeff(self._h, None), "tm_batch_set_site_coeff")
+            return
+        buf = np.ascontiguousarray(coeff, self.dtype) if isinstance(coeff, np.ndarray) and coeff.ndim == 1 \
+            else pack(coeff, self.inst, self.nf, self.dtype)
+        self._site_b = buf
+        T.check(T.lib().tm_batch_set_site_coeff(self._h, buf.ctypes.data_as(C.c_void_p)), "tm_batch_set_site_coeff")
+
+    def box_means(self, k, box, field=0):
+        """Kadanoff block means (L/box x L/box) of instance k's field."""
+        L = self.inst[k].L
+        out = np.zeros((L // box) * (L // box))
+        T.check(T.lib().tm_batch_box_means(self._h, k, field, box, out.ctypes.data_as(C.POINTER(C.c_double))),
+                "tm_batch_box_means")
+        return out.reshape(L // box, L // box)
+
     def power_spectrum(self, k, field=0, binwidth=0.5):
         """Radially averaged power spectrum of instance k's field (glow_up.py:752-827
         semantics); returns (kvals, power)."""

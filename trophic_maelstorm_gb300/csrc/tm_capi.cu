@@ -73,6 +73,7 @@ struct tm_batch {
     int cur = 0;
     void* aux = nullptr;        // Rietkerk P* (field-0 slots) / noise-off DP stage buffers
     void* kst[4] = {nullptr, nullptr, nullptr, nullptr};
+    void* site_b = nullptr;     // per-site loss coefficient (DP), packed like the state
     long long* d_step = nullptr;
     int64_t step = 0;
 
@@ -172,6 +173,7 @@ DornicArgs<T> dornic_args(const tm_batch* b, const T* in, T* out, const long lon
     DornicArgs<T> a{};
     a.in = in; a.out = out; a.it = b->tables(); a.tasks = b->d_tasks; a.n_tasks = b->n_tasks;
     a.step_base = step_base; a.step_off = step_off; a.rows_cap = b->rows_per_task;
+    a.site_b = (b->model == 0) ? (const T*)b->site_b : nullptr;
     if (b->model == 0) {
         const tm_dp_model& m = b->dpm;
         a.dcoef = (T)(m.D / (m.dx * m.dx));
@@ -466,7 +468,7 @@ int tm_batch_destroy(tm_batch* b)
     cudaSetDevice(b->ctx->device);
     cudaStreamSynchronize(b->ctx->stream);
     free_graphs(b);
-    cudaFree(b->buf[0]); cudaFree(b->buf[1]); cudaFree(b->aux);
+    cudaFree(b->buf[0]); cudaFree(b->buf[1]); cudaFree(b->aux); cudaFree(b->site_b);
     for (auto p : b->kst) cudaFree(p);
     cudaFree(b->d_step); cudaFree(b->d_off); cudaFree(b->d_fstride); cudaFree(b->d_L); cudaFree(b->d_seed);
     cudaFree(b->d_R); cudaFree(b->d_a0); cudaFree(b->d_astep); cudaFree(b->d_consts); cudaFree(b->d_alive);
@@ -768,6 +770,48 @@ int tm_batch_autotune(tm_batch* b, int steps_per_trial)
     cudaFree(save);
     if (rc) return rc;
     return tm_batch_set_launch(b, best_r, best_c);
+}
+
+int tm_batch_set_site_coeff(tm_batch* b, const void* host_coeff)
+{
+    if (!b || b->model != 0 || b->dpm.deterministic) return TM_ERR_INVALID;
+    TM_CUDA(cudaSetDevice(b->ctx->device));
+    TM_CUDA(cudaStreamSynchronize(b->ctx->stream));
+    if (!host_coeff) {
+        cudaFree(b->site_b);
+        b->site_b = nullptr;
+    } else {
+        if (!b->site_b && !cuda_ok(cudaMalloc(&b->site_b, (size_t)b->total * b->esize))) return TM_ERR_NOMEM;
+        TM_CUDA(cudaMemcpy(b->site_b, host_coeff, (size_t)b->total * b->esize, cudaMemcpyHostToDevice));
+    }
+    free_graphs(b);
+    return TM_OK;
+}
+
+int tm_batch_box_means(tm_batch* b, int k, int field, int box, double* out)
+{
+    if (!b || !out || k < 0 || k >= b->n_inst || field < 0 || field >= b->nf || box < 1) return TM_ERR_INVALID;
+    const int L = b->inst[k].L;
+    if (L % box != 0) return TM_ERR_INVALID;
+    TM_CUDA(cudaSetDevice(b->ctx->device));
+    const size_t nb = (size_t)(L / box) * (L / box);
+    int alive = 1;
+    if (b->model == 0) TM_CUDA(cudaMemcpy(&alive, b->d_alive + k, sizeof(int), cudaMemcpyDeviceToHost));
+    if (!alive) {
+        for (size_t i = 0; i < nb; ++i) out[i] = 0.0;
+        return TM_OK;
+    }
+    double* d = nullptr;
+    TM_CUDA(cudaMalloc(&d, nb * sizeof(double)));
+    const char* base = (const char*)b->buf[b->cur] + (size_t)(b->off[k] + field * b->fstride[k]) * b->esize;
+    cudaError_t e = b->precision == TM_FP64
+                        ? launch_box_means<double>((const double*)base, L, box, d, b->ctx->stream)
+                        : launch_box_means<float>((const float*)base, L, box, d, b->ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, nb * sizeof(double), cudaMemcpyDeviceToHost, b->ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->ctx->stream);
+    cudaFree(d);
+    TM_CUDA(e);
+    return TM_OK;
 }
 
 int tm_batch_power_spectrum(tm_batch* b, int k, int field, double binwidth, double* kvals, double* power,

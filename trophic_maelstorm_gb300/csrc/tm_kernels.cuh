@@ -37,6 +37,7 @@ struct DornicArgs {
     int sampler;                   // 0 exact, 1 Gaussian above 100, 2 mean (noise off)
     int cubic;
     int rows_cap;                  // rows of the largest task (<= kMaxRowsPerTask)
+    const T* site_b;               // per-site loss coefficient b_v (packed like the state) or nullptr
 };
 
 template <typename T>
@@ -70,6 +71,8 @@ cudaError_t launch_finalize(const double* partial, const int* task_begin, const 
 cudaError_t launch_consts(const double* a0, const double* astep, int n, double diff4, double sigma2, double dt,
                           const long long* step_base, long long step_off, Dc4* out, cudaStream_t s);
 cudaError_t launch_set_step(long long* d_step, long long v, cudaStream_t s);
+template <typename T>
+cudaError_t launch_box_means(const T* field, int L, int box, double* out, cudaStream_t s);
 template <typename T>
 cudaError_t launch_det_stage(const DetStageArgs<T>& a, cudaStream_t s);
 template <typename T>

@@ -146,16 +146,18 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
         __syncwarp();
         // pass 3: remainder, clamp, store
         if (act) {
+            const T* __restrict__ sb = A.site_b ? A.site_b + A.it.off[k] : nullptr;
             for (int r = 0; r < rows; ++r) {
                 const T rs = Wres[r * 32 + lane];
+                const T bi = sb ? sb[(long long)(y0 + r) * L + x] : A.b;
                 T res;
                 if (REM == 0) {
-                    res = rs / (T(1) + (A.b * rs) * A.dt);
+                    res = rs / (T(1) + (bi * rs) * A.dt);
                 } else if (REM == 1) {
-                    const T k1 = rem_f(rs, A.b, A.c, A.cubic);
-                    const T k2 = rem_f(rs + A.dt2 * k1, A.b, A.c, A.cubic);
-                    const T k3 = rem_f(rs + A.dt2 * k2, A.b, A.c, A.cubic);
-                    const T k4 = rem_f(rs + A.dt * k3, A.b, A.c, A.cubic);
+                    const T k1 = rem_f(rs, bi, A.c, A.cubic);
+                    const T k2 = rem_f(rs + A.dt2 * k1, bi, A.c, A.cubic);
+                    const T k3 = rem_f(rs + A.dt2 * k2, bi, A.c, A.cubic);
+                    const T k4 = rem_f(rs + A.dt * k3, bi, A.c, A.cubic);
                     res = rs + A.dt6 * (((k1 + T(2) * k2) + T(2) * k3) + k4);
                 } else {
                     res = rs;
@@ -228,6 +230,31 @@ cudaError_t launch_consts(const double* a0, const double* astep, int n, double d
 }
 
 __global__ void set_step_kernel(long long* d, long long v) { *d = v; }
+
+// Kadanoff block means (sde_RFT_2D...DEF.f:474-516): one thread per box x box
+// block, summed in row order in FP64.
+template <typename T>
+__global__ void box_means_kernel(const T* f, int L, int box, double* out)
+{
+    const int nb = L / box;
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb * nb) return;
+    const int by = b / nb, bx = b - by * nb;
+    double s = 0.0;
+    for (int y = 0; y < box; ++y)
+        for (int x = 0; x < box; ++x) s += (double)f[(long long)(by * box + y) * L + bx * box + x];
+    out[b] = s / ((double)box * (double)box);
+}
+
+template <typename T>
+cudaError_t launch_box_means(const T* field, int L, int box, double* out, cudaStream_t s)
+{
+    const int n = (L / box) * (L / box);
+    box_means_kernel<T><<<(n + 127) / 128, 128, 0, s>>>(field, L, box, out);
+    return cudaGetLastError();
+}
+template cudaError_t launch_box_means<float>(const float*, int, int, double*, cudaStream_t);
+template cudaError_t launch_box_means<double>(const double*, int, int, double*, cudaStream_t);
 
 cudaError_t launch_set_step(long long* d_step, long long v, cudaStream_t s)
 {
