@@ -405,8 +405,10 @@ __device__ __forceinline__ T poisson_exact(Stream<T>& g, T m, const SmemTab<T>& 
     if (m < T(32)) {
         const uint32_t w = g.u32();
         const T u = (T)w * T(0x1p-32);
-        T p = tm_exp(-m);
-        T q = (m < T(0.25)) ? tm_negexpm1(m) : T(1) - p;  // tm_negexpm1's own split
+        const bool small = m < T(0.25);                      // tm_negexpm1's own split
+        T p = small ? T(0) : tm_exp(-m);
+        T q = small ? tm_negexpm1(m) : T(1) - p;
+        if (small && u < q) p = tm_exp(-m);                   // e^-m only when the search starts
         T n = T(0);
         int it = 0;
         while (u < q && it < 200) {
@@ -515,9 +517,9 @@ __device__ __forceinline__ T dornic_draw(Stream<T>& g, T m, T mu1, T inv_lambda,
 }
 
 // Straight-line draw for the common case (FP32): one Philox block of four
-// words, Poisson by inversion finishing within kFastInv steps, shape >= 1, a
-// ziggurat normal accepted by its fast test and one Marsaglia-Tsang attempt
-// accepted by the squeeze.  Every step consumes the counter stream exactly as
+// words, Poisson by inversion finishing within kFastInv steps, a ziggurat
+// normal accepted by its fast test, one Marsaglia-Tsang attempt accepted by
+// the squeeze and, for shape < 1, the U^(1/k) boost from the next word.  Every step consumes the counter stream exactly as
 // dornic_draw does, so when it returns without deferring the value equals
 // dornic_draw's bit for bit; otherwise (*deferred) the caller recomputes the
 // site with dornic_draw.
@@ -552,8 +554,11 @@ __device__ __forceinline__ float dornic_draw_fast(uint64_t seed, uint32_t site, 
     if (draw) {
         if (!(m < 32.0f)) { deferred = true; return 0.0f; }
         const float u = (float)r.x * 0x1p-32f;
-        float p = tm_exp(-m);
-        float q = (m < 0.25f) ? tm_negexpm1(m) : 1.0f - p;
+        // e^-m is only needed once u < q; below m = 0.25 q has its own series
+        const bool small = m < 0.25f;
+        float p = small ? 0.0f : tm_exp(-m);
+        float q = small ? tm_negexpm1(m) : 1.0f - p;
+        if (small && u < q) p = tm_exp(-m);
         int it = 0;
         while (u < q && it < kFastInv) {
             ++it;
@@ -565,9 +570,11 @@ __device__ __forceinline__ float dornic_draw_fast(uint64_t seed, uint32_t site, 
     }
     const float k = mu1 + n;
     if (!(k > 0.0f)) return 0.0f;  // Gamma(0) = 0, no draw
-    if (k < 1.0f || (sampler == 1 && k > 100.0f)) { deferred = true; return 0.0f; }
-    const uint32_t wz = draw ? r.y : r.x, wu = draw ? r.z : r.y;
-    const float d = k - (float)(1.0 / 3.0);
+    if (sampler == 1 && k > 100.0f) { deferred = true; return 0.0f; }
+    const uint32_t wz = draw ? r.y : r.x, wu = draw ? r.z : r.y, wb = draw ? r.w : r.z;
+    const bool boost = k < 1.0f;            // Gamma(k) = Gamma(k+1) U^(1/k)
+    const float kk = boost ? k + 1.0f : k;
+    const float d = kk - (float)(1.0 / 3.0);
     const float c = 1.0f / sqrtf(9.0f * d);
     const int iz = (int)(wz & 127u);
     const int32_t hz = (int32_t)(wz >> 7) - (int32_t)(1 << 24);
@@ -580,7 +587,12 @@ __device__ __forceinline__ float dornic_draw_fast(uint64_t seed, uint32_t site, 
     const float u = ((float)(wu >> 8) + 0.5f) * 0x1p-24f;
     const float x2 = x * x;
     if (!(u < 1.0f - 0.0331f * (x2 * x2))) { deferred = true; return 0.0f; }
-    return (d * v) * inv_lambda;
+    float res = d * v;
+    if (boost) {
+        const float ub = ((float)(wb >> 8) + 0.5f) * 0x1p-24f;
+        res = res * tm_exp(tm_log_pos(ub) / k);
+    }
+    return res * inv_lambda;
 }
 
 template <typename T>

@@ -4,9 +4,10 @@
 // Rietkerk (rietkerk_bjork_FKE.cpp:2363-2444 stochastic remainder f_2Dor,
 // :1760-1856 noise-off f_2D): the W and O tendencies carry 5-point
 // Laplacians, so stage s needs stage s-1 values one site further out.  A CTA
-// loads a (32+8) x (16+8) region of [P*, W, O] (halo 4, periodic wrap) into
-// shared memory and runs all four stages there, each stage valid on a region
-// one site smaller, so the 32 x 16 interior comes out exact after stage 4.
+// loads a (64+8) x (16+8) region of [P*, W, O] (halo 4, periodic wrap) into
+// shared memory and runs all four stages there, stage s only on the region
+// inset by s+1 cells, so the 64 x 16 interior comes out exact after stage 4
+// with 1.25 stage evaluations per cell and stage.
 // The state is read and written once per step (plus the halo re-read, which
 // hits L2); the K1..K4 temporaries the reference keeps as full lattices
 // never leave the SM.
@@ -15,12 +16,54 @@
 
 namespace tmg {
 
+// Right-hand side at region cell c of S (f_2Dor, or f_2D when DET); R per instance.
 template <typename T, bool DET>
-__global__ void __launch_bounds__(RK_THREADS) rk4_tile_kernel(const RK4Args<T> A)
+__device__ __forceinline__ void rk_rhs_cell(const RK4Args<T>& A, const T* S, int c, T R, T& fP, T& fW, T& fO)
 {
-    __shared__ T X0[3][RK_RN];
-    __shared__ T M[3][RK_RN];
-    constexpr int PER = (RK_RN + RK_THREADS - 1) / RK_THREADS;
+    const int cn = c - RK_RX, cs = c + RK_RX, cw = c - 1, ce = c + 1;
+    const T* SP = S;
+    const T* SW = S + RK_RN;
+    const T* SO = S + 2 * RK_RN;
+    const T Pc = SP[c], Wc = SW[c], Oc = SO[c];
+    const T upt_num = (A.gmax * Wc) * Pc;
+    const T wk = Wc + A.k1;
+    T infil, upt;
+    if constexpr (sizeof(T) == 8) {
+        // the reference's own expressions
+        infil = ((A.alpha * (Pc + A.k2W0)) / (Pc + A.k2)) * Oc;
+        fP = ((A.cgmax * Wc) * Pc) / wk;
+        upt = upt_num / wk;
+    } else {
+        // FP32: two reciprocals instead of three divisions
+        const T iwk = T(1) / wk;
+        infil = ((A.alpha * (Pc + A.k2W0)) * (T(1) / (Pc + A.k2))) * Oc;
+        fP = ((A.cgmax * Wc) * Pc) * iwk;
+        upt = upt_num * iwk;
+    }
+    const T lapW = (((SW[cn] + SW[cs]) + SW[cw]) + SW[ce]) - T(4) * Wc;
+    const T lapO = (((SO[cn] + SO[cs]) + SO[cw]) + SO[ce]) - T(4) * Oc;
+    if (DET) {
+        const T lapP = (((SP[cn] + SP[cs]) + SP[cw]) + SP[ce]) - T(4) * Pc;
+        fP = (fP - A.d * Pc) + A.DPx * lapP;
+    }
+    fW = ((infil - upt) - A.rW * Wc) + A.DWx * lapW;
+    fO = (R - infil) + A.DOx * lapO;
+}
+
+// One CTA per tile (persistent over tiles).  Stage s (0..3) is evaluated on
+// the region inset by s+1 cells -- exactly the cells whose stage-s value an
+// interior cell depends on -- so the interior is exact after stage 3.  Stage
+// inputs ping-pong between two shared buffers, so each stage needs one barrier
+// and no value is held in registers across it.
+template <typename T, bool DET>
+__global__ void __launch_bounds__(RK_THREADS, 3) rk4_tile_kernel(const RK4Args<T> A)
+{
+    extern __shared__ __align__(16) unsigned char rk_smem[];
+    T* const X0 = reinterpret_cast<T*>(rk_smem);          // [3][RK_RN] stage-0 input
+    T* const MA = X0 + 3 * RK_RN;                           // [3][RK_RN] stage inputs (ping)
+    T* const MB = MA + 3 * RK_RN;                           // [3][RK_RN] (pong)
+    T* const ACC = MB + 3 * RK_RN;                          // [3][RK_TX*RK_TY] weighted sum of K
+    constexpr int NI = RK_TX * RK_TY;
     const int tid = threadIdx.x;
     for (int t = blockIdx.x; t < A.n_tasks; t += gridDim.x) {
         const int4 tk = A.tasks[t];
@@ -33,101 +76,62 @@ __global__ void __launch_bounds__(RK_THREADS) rk4_tile_kernel(const RK4Args<T> A
         const T* __restrict__ P0 = (DET ? A.in : A.pstar) + off;
         const T* __restrict__ W0 = A.in + off + fs;
         const T* __restrict__ O0 = A.in + off + 2 * fs;
-        __syncthreads();  // previous task finished with the tile
+        __syncthreads();  // previous tile done with shared memory
         for (int c = tid; c < RK_RN; c += RK_THREADS) {
             const int ry = c / RK_RX, rx = c - ry * RK_RX;
             int gy = (y0 - RK_H + ry) % L; if (gy < 0) gy += L;
             int gx = (x0 - RK_H + rx) % L; if (gx < 0) gx += L;
             const long long gi = (long long)gy * L + gx;
-            X0[0][c] = P0[gi];
-            X0[1][c] = W0[gi];
-            X0[2][c] = O0[gi];
+            X0[c] = P0[gi];
+            X0[RK_RN + c] = W0[gi];
+            X0[2 * RK_RN + c] = O0[gi];
         }
         __syncthreads();
-        T acc[PER][3];
-        T kv[PER][3];
-#pragma unroll
-        for (int j = 0; j < PER; ++j) { acc[j][0] = acc[j][1] = acc[j][2] = T(0); }
 #pragma unroll
         for (int s = 0; s < 4; ++s) {
-            const T (*S)[RK_RN] = (s == 0) ? X0 : M;
-#pragma unroll
-            for (int j = 0; j < PER; ++j) {
-                const int c = tid + j * RK_THREADS;
-                kv[j][0] = kv[j][1] = kv[j][2] = T(0);
-                if (c < RK_RN) {
-                    const int ry = c / RK_RX, rx = c - ry * RK_RX;
-                    if (ry >= 1 && ry < RK_RY - 1 && rx >= 1 && rx < RK_RX - 1) {
-                        const int cn = c - RK_RX, cs = c + RK_RX, cw = c - 1, ce = c + 1;
-                        const T Pc = S[0][c], Wc = S[1][c], Oc = S[2][c];
-                        const T upt_num = (A.gmax * Wc) * Pc;
-                        const T wk = Wc + A.k1;
-                        T infil, fP, upt;
-                        if constexpr (sizeof(T) == 8) {
-                            // the reference's own expressions
-                            infil = ((A.alpha * (Pc + A.k2W0)) / (Pc + A.k2)) * Oc;
-                            fP = ((A.cgmax * Wc) * Pc) / wk;
-                            upt = upt_num / wk;
-                        } else {
-                            // FP32: two reciprocals instead of three divisions
-                            const T iwk = T(1) / wk;
-                            infil = ((A.alpha * (Pc + A.k2W0)) * (T(1) / (Pc + A.k2))) * Oc;
-                            fP = ((A.cgmax * Wc) * Pc) * iwk;
-                            upt = upt_num * iwk;
-                        }
-                        const T lapW = (((S[1][cn] + S[1][cs]) + S[1][cw]) + S[1][ce]) - T(4) * Wc;
-                        const T lapO = (((S[2][cn] + S[2][cs]) + S[2][cw]) + S[2][ce]) - T(4) * Oc;
-                        if (DET) {
-                            const T lapP = (((S[0][cn] + S[0][cs]) + S[0][cw]) + S[0][ce]) - T(4) * Pc;
-                            fP = (fP - A.d * Pc) + A.DPx * lapP;
-                        }
-                        kv[j][0] = fP;
-                        kv[j][1] = ((infil - upt) - A.rW * Wc) + A.DWx * lapW;
-                        kv[j][2] = (R - infil) + A.DOx * lapO;
-                    }
+            const T* S = (s == 0) ? X0 : ((s & 1) ? MA : MB);
+            T* D = (s & 1) ? MB : MA;
+            const T coef = (s == 2) ? A.dt : A.dt2;
+            const int in = s + 1;
+            const int w = RK_RX - 2 * in, h = RK_RY - 2 * in;
+            for (int q = tid; q < w * h; q += RK_THREADS) {
+                const int ry = in + q / w, rx = in + q % w;
+                const int c = ry * RK_RX + rx;
+                T k0, k1, k2;
+                rk_rhs_cell<T, DET>(A, S, c, R, k0, k1, k2);
+                const int ly = ry - RK_H, lx = rx - RK_H;
+                if (ly >= 0 && ly < RK_TY && lx >= 0 && lx < RK_TX) {
+                    const int a = ly * RK_TX + lx;
                     if (s == 0) {
-                        acc[j][0] = kv[j][0]; acc[j][1] = kv[j][1]; acc[j][2] = kv[j][2];
+                        ACC[a] = k0; ACC[NI + a] = k1; ACC[2 * NI + a] = k2;
                     } else if (s == 3) {
-                        acc[j][0] = acc[j][0] + kv[j][0]; acc[j][1] = acc[j][1] + kv[j][1]; acc[j][2] = acc[j][2] + kv[j][2];
+                        ACC[a] = ACC[a] + k0; ACC[NI + a] = ACC[NI + a] + k1; ACC[2 * NI + a] = ACC[2 * NI + a] + k2;
                     } else {
-                        acc[j][0] = acc[j][0] + T(2) * kv[j][0];
-                        acc[j][1] = acc[j][1] + T(2) * kv[j][1];
-                        acc[j][2] = acc[j][2] + T(2) * kv[j][2];
+                        ACC[a] = ACC[a] + T(2) * k0; ACC[NI + a] = ACC[NI + a] + T(2) * k1;
+                        ACC[2 * NI + a] = ACC[2 * NI + a] + T(2) * k2;
                     }
                 }
-            }
-            if (s < 3) {
-                const T coef = (s == 2) ? A.dt : A.dt2;
-                __syncthreads();  // all reads of the stage input done
-#pragma unroll
-                for (int j = 0; j < PER; ++j) {
-                    const int c = tid + j * RK_THREADS;
-                    if (c < RK_RN) {
-                        M[0][c] = X0[0][c] + coef * kv[j][0];
-                        M[1][c] = X0[1][c] + coef * kv[j][1];
-                        M[2][c] = X0[2][c] + coef * kv[j][2];
-                    }
+                if (s < 3) {
+                    D[c] = X0[c] + coef * k0;
+                    D[RK_RN + c] = X0[RK_RN + c] + coef * k1;
+                    D[2 * RK_RN + c] = X0[2 * RK_RN + c] + coef * k2;
                 }
-                __syncthreads();
             }
+            __syncthreads();
         }
         unsigned st = 0;
+        for (int a = tid; a < NI; a += RK_THREADS) {
+            const int ly = a / RK_TX, lx = a - ly * RK_TX;
+            const int gy = y0 + ly, gx = x0 + lx;
+            if (gy < L && gx < L) {
+                const int c = (ly + RK_H) * RK_RX + lx + RK_H;
+                const long long gi = off + (long long)gy * L + gx;
 #pragma unroll
-        for (int j = 0; j < PER; ++j) {
-            const int c = tid + j * RK_THREADS;
-            if (c < RK_RN) {
-                const int ry = c / RK_RX, rx = c - ry * RK_RX;
-                const int ly = ry - RK_H, lx = rx - RK_H;
-                const int gy = y0 + ly, gx = x0 + lx;
-                if (ly >= 0 && ly < RK_TY && lx >= 0 && lx < RK_TX && gy < L && gx < L) {
-                    const long long gi = off + (long long)gy * L + gx;
-#pragma unroll
-                    for (int f = 0; f < 3; ++f) {
-                        T v = X0[f][c] + A.dt6 * acc[j][f];
-                        if (v < A.ceps && v >= A.clo) v = T(0);
-                        st |= value_status(v);
-                        A.out[gi + f * fs] = v;
-                    }
+                for (int f = 0; f < 3; ++f) {
+                    T v = X0[f * RK_RN + c] + A.dt6 * ACC[f * NI + a];
+                    if (v < A.ceps && v >= A.clo) v = T(0);
+                    st |= value_status(v);
+                    A.out[gi + f * fs] = v;
                 }
             }
         }
@@ -139,8 +143,17 @@ template <typename T>
 cudaError_t launch_rk4(const RK4Args<T>& a, bool det, int grid, cudaStream_t s)
 {
     if (a.n_tasks <= 0) return cudaSuccess;
-    if (det) rk4_tile_kernel<T, true><<<grid, RK_THREADS, 0, s>>>(a);
-    else rk4_tile_kernel<T, false><<<grid, RK_THREADS, 0, s>>>(a);
+    const size_t smem = (9 * (size_t)RK_RN + 3 * (size_t)RK_TX * RK_TY) * sizeof(T);
+    static bool attr[2] = {false, false};
+    cudaError_t e = cudaSuccess;
+    if (!attr[det ? 1 : 0]) {
+        e = det ? cudaFuncSetAttribute(rk4_tile_kernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                : cudaFuncSetAttribute(rk4_tile_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr[det ? 1 : 0] = true;
+    }
+    if (det) rk4_tile_kernel<T, true><<<grid, RK_THREADS, smem, s>>>(a);
+    else rk4_tile_kernel<T, false><<<grid, RK_THREADS, smem, s>>>(a);
     return cudaGetLastError();
 }
 template cudaError_t launch_rk4<float>(const RK4Args<float>&, bool, int, cudaStream_t);
