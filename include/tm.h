@@ -240,6 +240,28 @@ int tm_power_spectrum_device(const void* dev_field, int precision, int L, double
 int tm_batch_power_spectrum(tm_batch* b, int k, int field, double binwidth, double* kvals, double* power,
                             int max_bins, int* n_bins);
 
+/* -- consumer movement: FKE advection-diffusion ---------------------------
+ * Replaces advdiff_FKE_MultiSp (simulations/Rietkerk_FPE/rietkerk_bjork_FKE.cpp:
+ * 3614-3695) and its CUDA kernel updateMovement (kernel_advdiff_FKE2D.cu:92-180)
+ * for one consumer field on an L x L periodic lattice.  Every site with
+ * rho >= eps moves its mass through the separable Gaussian stencils gD
+ * (diffusion, gD[0..RD]) and gV (advection, gV[0..RV]): fraction gamma^2 by
+ * diffusion around the site, (1-gamma)^2 by advection around the site shifted
+ * by round(v * pref) in each axis (x = row, y = column), and gamma(1-gamma)
+ * by each of the two mixed products; sites below eps end as 0.  The stencils
+ * and pref are what set_global_FKE_params / precompute_gaussian
+ * (rietkerk_bjork_FKE.cpp:195-338, :1735-1749) give for the species.
+ *   dev_rho, dev_gamma, dev_vx, dev_vy  device, L*L row-major, `precision`
+ *   dev_out  device, L*L; receives the moved field (distinct from the inputs)
+ *   gD, gV   host arrays; RD, RV <= 63; 1 <= L <= 46340
+ * Computed as a gather (each target sums its sources), so the result has no
+ * atomics and does not depend on scheduling; it equals the reference's
+ * scatter up to the order of the floating-point additions.  Allocates
+ * scratch of 16*L*L bytes and synchronises `stream`. */
+int tm_fke_advdiff_device(const void* dev_rho, const void* dev_gamma, const void* dev_vx, const void* dev_vy,
+                          int precision, int L, double pref, double eps, const double* gD, int RD,
+                          const double* gV, int RV, void* dev_out, void* stream);
+
 /* Packed-layout geometry without a batch (for callers that pack host buffers
  * before creating one): offsets[k] and the total, for nf fields per instance. */
 int64_t tm_layout(const tm_instance* inst, int n_inst, int nf, int64_t* offsets, int64_t* field_strides);

@@ -77,6 +77,8 @@ def lib():
                                                        C.c_int, dp, dp, ptr, u32p]
             getattr(L, f"tmo_rk_run_{nm}").argtypes = [C.POINTER(RKParams), C.c_int, C.c_uint64, ptr, C.c_int64, i64p,
                                                        C.c_int, dp, dp, ptr, u32p]
+        L.tmo_fke_advdiff_f64.argtypes = [C.c_int, dp, dp, dp, dp, C.c_double, C.c_double, dp, C.c_int, dp, C.c_int,
+                                          dp]
         L.tmo_dornic_consts_compute.argtypes = [C.c_double] * 5 + [C.POINTER(DornicConsts)]
         L.tmo_dp_batch_run_f32.argtypes = [C.POINTER(DPParams), C.POINTER(C.c_int), C.POINTER(C.c_uint64),
                                            C.POINTER(fp), C.c_int, C.c_int64, C.c_int]
@@ -238,3 +240,14 @@ def dp_batch_run_f32(params, Ls, seeds, fields, n_steps, n_threads=0):
     ptrs = (C.POINTER(C.c_float) * n)(*[_ptr(f) for f in fields])
     rc = lib().tmo_dp_batch_run_f32(P, Larr, S, ptrs, n, n_steps, n_threads)
     assert rc == 0
+
+
+def fke_advdiff(rho, gamma, vx, vy, pref, gD, gV, eps=1e-10):
+    L = int(round(np.sqrt(rho.size)))
+    a = [np.ascontiguousarray(x, np.float64).ravel() for x in (rho, gamma, vx, vy)]
+    gD = np.ascontiguousarray(gD, np.float64)
+    gV = np.ascontiguousarray(gV, np.float64)
+    out = np.zeros(L * L)
+    lib().tmo_fke_advdiff_f64(L, _ptr(a[0]), _ptr(a[1]), _ptr(a[2]), _ptr(a[3]), pref, eps, _ptr(gD), len(gD) - 1,
+                              _ptr(gV), len(gV) - 1, _ptr(out))
+    return out

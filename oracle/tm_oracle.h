@@ -151,6 +151,10 @@ int tmo_rk_run_f32(const tmo_rk_params* p, int L, uint64_t seed, const float* f0
                    int64_t n_steps, const int64_t* meas_steps, int n_meas,
                    double* out_mean, double* out_active, float* f_final, uint32_t* status);
 
+/* FKE advection-diffusion of a consumer field (rietkerk_bjork_FKE.cpp:3614-3695). */
+void tmo_fke_advdiff_f64(int L, const double* rho, const double* gam, const double* vx, const double* vy,
+                         double pref, double eps, const double* gD, int RD, const double* gV, int RV, double* out);
+
 /* Many independent DP instances on host threads (OpenMP): the CPU baseline. */
 int tmo_dp_batch_run_f32(const tmo_dp_params* p /* n_inst */, const int* L, const uint64_t* seed,
                          float* const* rho /* in: initial, out: final */, int n_inst,

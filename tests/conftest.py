@@ -23,4 +23,5 @@ def oracle():
 def golden():
     import numpy as np
     d = os.path.join(REPO, "tests", "golden")
-    return {"pins": np.load(os.path.join(d, "ref_pins.npz")), "ens": np.load(os.path.join(d, "ref_dp_ensemble.npz"))}
+    return {"pins": np.load(os.path.join(d, "ref_pins.npz")), "ens": np.load(os.path.join(d, "ref_dp_ensemble.npz")),
+            "fke": np.load(os.path.join(d, "ref_fke.npz"))}

@@ -13,6 +13,8 @@ ref_pins.npz       deterministic outputs of the reference's stage functions
                    4th-order noise-off DP RK4, logarithm10_time_bins).
 ref_csv.npz        files written by the reference's own save_frame / save_prelimframe
                    (multiSPDP.cpp:1493-1643), byte for byte.
+ref_fke.npz        the consumer species' FKE advection-diffusion (advdiff_FKE_MultiSp,
+                   rietkerk_bjork_FKE.cpp:3614-3695) with its stencils.
 ref_dp_ensemble.npz  per-replicate trajectories of percolationDornic_2D
                    (stochasticSPDP.cpp:940), one replicate per call.  The
                    reference seeds std::mt19937_64 from std::random_device, so
@@ -37,13 +39,20 @@ def _p(a):
     return a.ctypes.data_as(dp)
 
 
-def load():
+def load(names=("dp", "rietkerk", "multisp")):
+    # the FKE harness is a -DSPB=2 build of the same sources as the -DSPB=1 one:
+    # their header-defined globals clash, so it is loaded in its own process
     libs = {}
-    for nm in ("dp", "rietkerk", "multisp"):
+    for nm in names:
         path = os.path.join(REF, f"libref_{nm}.so")
         if not os.path.exists(path):
             sys.exit(f"missing {path}: run `make -C oracle ref` first")
         libs[nm] = C.CDLL(path)
+    if "fke" in libs:
+        ip = C.POINTER(C.c_int)
+        libs["fke"].ref_fke_advdiff.argtypes = [dp, dp, dp, dp, C.c_int] + [C.c_double] * 5 + \
+            [dp, dp, ip, dp, ip, dp, C.c_int]
+        return libs
     d = libs["dp"]
     d.ref_percolation_dornic.argtypes = [dp, C.c_int, dp] + [C.c_double] * 7 + [C.c_int, C.c_int, dp, C.c_int]
     d.ref_perc_nodiff.argtypes = [dp, C.c_int, dp] + [C.c_double] * 6 + [C.c_int, dp, C.c_int]
@@ -154,7 +163,36 @@ def csv_writers(libs, rng):
     return out
 
 
+def fke(libs, rng):
+    """advdiff_FKE_MultiSp (rietkerk_bjork_FKE.cpp:3614-3695) on the grazer field,
+    with the parameters and stencils set_global_FKE_params / precompute_gaussian
+    give; L = 9 makes the stencils wrap the lattice more than once."""
+    out = {}
+    for tag, L, Dg, vg, sg, dta, vmax in (("a", 24, 1.0, 1.0, 1.5, 1.0, 3.0), ("b", 9, 1.0, 2.0, 2.0, 1.0, 2.0)):
+        rho = rng.uniform(0, 2, L * L)
+        rho[rng.random(L * L) < 0.2] = 0.0
+        rho[3] = 1e-12                       # below the reference's epsilon: not moved
+        gam = rng.uniform(0, 1, L * L)
+        vx = rng.uniform(-vmax, vmax, L * L)
+        vy = rng.uniform(-vmax, vmax, L * L)
+        o = np.zeros(L * L)
+        gD = np.zeros(64); gV = np.zeros(64)
+        RD = C.c_int(); RV = C.c_int(); pref = C.c_double()
+        rc = libs["fke"].ref_fke_advdiff(_p(rho), _p(gam), _p(vx), _p(vy), L, Dg, vg, sg, dta, 1.0, _p(o), _p(gD),
+                                         C.byref(RD), _p(gV), C.byref(RV), C.byref(pref), 64)
+        assert rc == 0, rc
+        out.update({f"fke_{tag}_rho": rho, f"fke_{tag}_gamma": gam, f"fke_{tag}_vx": vx, f"fke_{tag}_vy": vy,
+                    f"fke_{tag}_out": o, f"fke_{tag}_gD": gD[:RD.value + 1].copy(),
+                    f"fke_{tag}_gV": gV[:RV.value + 1].copy(), f"fke_{tag}_meta": np.array([L, pref.value])})
+    return out
+
+
 def main():
+    if "--fke" in sys.argv:
+        np.savez_compressed(os.path.join(HERE, "ref_fke.npz"), **fke(load(("fke",)), np.random.default_rng(11)))
+        return
+    import subprocess
+    subprocess.run([sys.executable, os.path.abspath(__file__), "--fke"], check=True)
     libs = load()
     rng = np.random.default_rng(20261203)
     np.savez_compressed(os.path.join(HERE, "ref_pins.npz"), **pins(libs, rng))

@@ -165,3 +165,43 @@ def test_box_means(tmg, ctx, precision):
             want = f[field].astype(np.float64).reshape(L // box, box, L // box, box).mean(axis=(1, 3))
             np.testing.assert_allclose(got, want, rtol=1e-12)
     b.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32"])
+@pytest.mark.parametrize("tag,D,v,sigma", [("a", 1.0, 1.0, 1.5), ("b", 1.0, 2.0, 2.0)])
+def test_fke_advdiff_matches_reference_fixture(tmg, oracle, precision, tag, D, v, sigma):
+    """Consumer movement (advdiff_FKE_MultiSp) on the reference's own fixture, L = 24
+    and L = 9 (stencils wrapping the lattice): the gather sums in another order than
+    the reference's scatter, so FP64 agrees to rounding, FP32 to single precision."""
+    pytest.importorskip("torch")
+    g = np.load(os.path.join(REPO, "tests", "golden", "ref_fke.npz"))
+    L = int(g[f"fke_{tag}_meta"][0])
+    fields = [g[f"fke_{tag}_{k}"].reshape(L, L) for k in ("rho", "gamma", "vx", "vy")]
+    p = tmg.fke_parameters(D, v, 1.0, sigma)
+    dtype = np.float64 if precision == 0 else np.float32
+    got = tmg.fke_advdiff(*[f.astype(dtype) for f in fields], p, precision=precision)
+    want = g[f"fke_{tag}_out"].reshape(L, L)
+    if precision == 0:
+        np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-15)
+    else:
+        np.testing.assert_allclose(got, want, rtol=2e-5, atol=1e-6 * want.max())
+
+
+@pytest.mark.parametrize("L,v", [(7, 3.0), (64, 1.0), (200, 4.0)])
+def test_fke_advdiff_matches_oracle(tmg, oracle, L, v):
+    """FP64 gather against the oracle's scatter on larger lattices: windowed gather
+    (L = 64, 200) and the whole-lattice case (L = 7); extinct sites and a site
+    just below eps included."""
+    pytest.importorskip("torch")
+    rng = np.random.default_rng(L)
+    rho = rng.uniform(0, 3, (L, L))
+    rho[rng.random((L, L)) < 0.3] = 0.0
+    rho[0, 1] = 5e-11
+    gam = rng.uniform(0, 1, (L, L))
+    vx = rng.uniform(-v, v, (L, L))
+    vy = rng.uniform(-v, v, (L, L))
+    p = tmg.fke_parameters(1.0, v, 1.0, 1.2)
+    got = tmg.fke_advdiff(rho, gam, vx, vy, p)
+    want = oracle.fke_advdiff(rho, gam, vx, vy, p.pref, p.gD, p.gV).reshape(L, L)
+    np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-14)
+    assert got.sum() == pytest.approx(rho[rho >= 1e-10].sum(), rel=1e-12)

@@ -91,3 +91,34 @@ def test_dp_ensemble_matches_reference(oracle, golden, tag, n_rep):
             assert abs(ps - pr) < 3.5 * se_s, (tag, j)
         if M[:, j].std() > 0 and R[:, j].std() > 0:
             assert stats.ks_2samp(M[:, j], R[:, j]).pvalue > 0.01 / n_t, (tag, j)
+
+
+# (tag, D, v, sigma, dt_adv) of the two cases in ref_fke.npz: L = 24, and L = 9
+# where the stencils wrap the lattice more than once
+FKE_CASES = [("a", 1.0, 1.0, 1.5, 1.0), ("b", 1.0, 2.0, 2.0, 1.0)]
+
+
+@pytest.mark.parametrize("tag,D,v,sigma,dt_adv", FKE_CASES, ids=[c[0] for c in FKE_CASES])
+def test_fke_parameters_match_reference(golden, tag, D, v, sigma, dt_adv):
+    """fke_parameters restates set_global_FKE_params / precompute_gaussian: same
+    prefactor and stencils, bit for bit."""
+    from trophic_maelstorm_gb300 import api
+    g = golden["fke"]
+    p = api.fke_parameters(D, v, dt_adv, sigma)
+    assert p.pref == g[f"fke_{tag}_meta"][1]
+    assert np.array_equal(p.gD, g[f"fke_{tag}_gD"]) and np.array_equal(p.gV, g[f"fke_{tag}_gV"])
+
+
+@pytest.mark.parametrize("tag", ["a", "b"])
+def test_fke_advdiff_matches_reference(oracle, golden, tag):
+    """The oracle's scatter (advdiff_FKE_MultiSp order) equals the reference bit for bit."""
+    g = golden["fke"]
+    L = int(g[f"fke_{tag}_meta"][0])
+    sh = (L, L)
+    out = oracle.fke_advdiff(g[f"fke_{tag}_rho"].reshape(sh), g[f"fke_{tag}_gamma"].reshape(sh),
+                             g[f"fke_{tag}_vx"].reshape(sh), g[f"fke_{tag}_vy"].reshape(sh),
+                             float(g[f"fke_{tag}_meta"][1]), g[f"fke_{tag}_gD"], g[f"fke_{tag}_gV"])
+    assert np.array_equal(out.reshape(-1), g[f"fke_{tag}_out"])
+    # mass is conserved up to the sites below eps, which the reference drops
+    rho = g[f"fke_{tag}_rho"]
+    assert out.sum() == pytest.approx(rho[rho >= 1e-10].sum(), rel=1e-12)

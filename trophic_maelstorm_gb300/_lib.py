@@ -27,7 +27,7 @@ EXPORTS = (
     "tm_batch_download_device", "tm_batch_snapshot", "tm_batch_advance", "tm_batch_enqueue_steps",
     "tm_batch_set_launch", "tm_batch_get_launch", "tm_batch_autotune", "tm_run_dp", "tm_run_rietkerk",
     "tm_layout", "tm_observe_noalloc", "tm_power_spectrum_device", "tm_batch_power_spectrum",
-    "tm_batch_set_site_coeff", "tm_batch_box_means",
+    "tm_batch_set_site_coeff", "tm_batch_box_means", "tm_fke_advdiff_device",
 )
 
 
@@ -106,6 +106,8 @@ def lib():
                                         C.c_int),
             "tm_batch_set_site_coeff": ([vp, vp], C.c_int),
             "tm_batch_box_means": ([vp, C.c_int, C.c_int, C.c_int, dp], C.c_int),
+            "tm_fke_advdiff_device": ([vp, vp, vp, vp, C.c_int, C.c_int, C.c_double, C.c_double, dp, C.c_int, dp,
+                                       C.c_int, vp, vp], C.c_int),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)

@@ -8,8 +8,10 @@ appends rows {a, L, t, <<rho>_x>_r, Var, #surviving runs, #active sites, #surv a
 for t = 0, dt, ... <= 1 and for every t in t_meas.  `percolation_dornic_2d`
 below takes the same arguments (plus a seed and a precision) and returns the
 same rows, computed by one batched GPU run of all r replicates.
-`critical_exp_delta` is the a-sweep around it (stochasticSPDP.cpp:1309-1422),
-`rietkerk_dornic_2d` the Rietkerk counterpart (rietkerk_bjork_FKE.cpp:3697).
+`critical_exp_delta` is the a-sweep around it (stochasticSPDP.cpp:1309-1422).
+A `Batch` of `rietkerk_model()` runs the three-field Rietkerk step that
+rietkerk_DorFPE_2D_MultiSp (rietkerk_bjork_FKE.cpp:3697) takes per time step;
+`fke_advdiff` is that driver's consumer movement (advdiff_FKE_MultiSp).
 """
 from __future__ import annotations
 
@@ -282,6 +284,85 @@ def pattern_wavelength(L, kvals, power):
     """Wavelength (lattice units) at the peak of a radial power spectrum: L / k_peak."""
     p = np.where(np.isfinite(power), power, -np.inf)
     return float(L) / float(kvals[int(np.argmax(p))])
+
+
+# ------------------------------------------------------ consumer movement (FKE)
+def _reference_pi():
+    """The reference's PI: 15 terms of the Bailey-Borwein-Plouffe series summed
+    from the smallest (CalculatePi<14>, rietkerk_bjork_basic.h:243-259, :284)."""
+    s = 0.0
+    for n in range(15):
+        s = (1.0 / 16 ** n) * (4.0 / (8 * n + 1.0) - 2.0 / (8 * n + 4.0) - 1.0 / (8 * n + 5.0)
+                               - 1.0 / (8 * n + 6.0)) + s
+    return s
+
+
+def gaussian_stencil(sigma, rbound):
+    """precompute_gaussian (rietkerk_bjork_FKE.cpp:1735-1749): the one-sided
+    Gaussian exp(-x^2 / 2 sigma^2) / (sqrt(2 pi) sigma) for x = 0..rbound,
+    renormalised so that the two-sided stencil sums to 1."""
+    factor = 1.0 / (math.sqrt(2 * _reference_pi()) * sigma)
+    st = np.empty(rbound + 1)
+    tot = 0.0
+    for x in range(rbound + 1):
+        st[x] = factor * math.exp(-0.5 * (x * x) / (sigma * sigma))
+        tot += 2 * st[x] if x > 0 else st[0]
+    return st / tot
+
+
+@dataclass
+class FKEParams:
+    pref: float          # mu_vel_prefactor: shift = round(v * pref) lattice sites
+    RD: int              # diffusion stencil bound (sites)
+    RV: int              # advection stencil bound (sites)
+    gD: np.ndarray       # diffusion stencil, RD + 1 values
+    gV: np.ndarray       # advection stencil, RV + 1 values
+
+
+def fke_parameters(D, v, dt_adv, sigma, dx=1.0, CI=4):
+    """set_global_FKE_params (rietkerk_bjork_FKE.cpp:195-338, displacement-
+    invariant default) for one consumer species: velocity relaxation beta =
+    3 / dt_adv, diffusion width sqrt(2 D dt_adv), the OU displacement width of
+    the velocity process, bounds int(CI * width / dx), and the shift prefactor
+    (dt_adv - (1 - e^{-beta dt_adv}) / beta) / dx.  Both stencils are built with
+    the species' `sigma`, as the reference's caller does (rietkerk_bjork_FKE.cpp:
+    3764-3772)."""
+    beta = 3.0 / dt_adv
+    e1 = math.exp(-beta * dt_adv)
+    e2 = math.exp(-2 * beta * dt_adv)
+    sv = math.sqrt(2 * beta * 1 * abs(v))
+    sigma_D = math.sqrt(2 * D * dt_adv)
+    svx = (sv / beta) * math.sqrt(dt_adv + (1 / (2 * beta)) * (1 - e2) - (2 / beta) * (1 - e1))
+    RD = int(CI * sigma_D / dx)
+    RV = int(CI * svx / dx)
+    pref = (1 / dx) * (dt_adv - ((1 - e1) / beta))
+    return FKEParams(pref, RD, RV, gaussian_stencil(sigma, RD), gaussian_stencil(sigma, RV))
+
+
+def fke_advdiff(rho, gamma, vx, vy, params: FKEParams, eps=1e-10, precision=T.TM_FP64, device=0):
+    """One FKE advection-diffusion of a consumer field (advdiff_FKE_MultiSp,
+    rietkerk_bjork_FKE.cpp:3614-3695) through tm_fke_advdiff_device.  rho, gamma,
+    vx, vy are L x L arrays (numpy, or CUDA torch tensors of the precision's
+    dtype, which are used in place); returns the moved field in the same kind."""
+    import torch
+    dt = torch.float64 if precision == T.TM_FP64 else torch.float32
+    as_numpy = isinstance(rho, np.ndarray)
+    dev = torch.device("cuda", device)
+    ts = [torch.as_tensor(np.ascontiguousarray(a), dtype=dt).to(dev) if as_numpy else a.contiguous()
+          for a in (rho, gamma, vx, vy)]
+    L = ts[0].shape[0]
+    if any(t.shape != (L, L) or t.dtype != dt or t.device != dev for t in ts):
+        raise T.TMError(T.TM_ERR_INVALID, "fke_advdiff: four L x L fields of one dtype on one device")
+    out = torch.empty_like(ts[0])
+    gD = np.ascontiguousarray(params.gD, np.float64)
+    gV = np.ascontiguousarray(params.gV, np.float64)
+    with torch.cuda.device(dev):
+        s = torch.cuda.current_stream(dev)
+        T.check(T.lib().tm_fke_advdiff_device(*(t.data_ptr() for t in ts), precision, L, params.pref, eps,
+                                              gD.ctypes.data_as(C.POINTER(C.c_double)), len(gD) - 1,
+                                              gV.ctypes.data_as(C.POINTER(C.c_double)), len(gV) - 1,
+                                              out.data_ptr(), s.cuda_stream), "tm_fke_advdiff_device")
+    return out.cpu().numpy() if as_numpy else out
 
 
 def run_dp(ctx, model, inst, init_packed, n_steps, meas_steps, precision):
