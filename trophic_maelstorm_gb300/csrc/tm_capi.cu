@@ -23,12 +23,6 @@
 
 using namespace tmg;
 
-struct tm_ctx {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    int num_sms = 0;
-};
-
 namespace {
 
 constexpr int kGraphSteps = 32;

@@ -4,6 +4,13 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+// A context: one device and the stream every call on it launches on (tm_create).
+struct tm_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int num_sms = 0;
+};
+
 namespace tmg {
 
 // Dornic constants of one instance: lambda e^{beta dt}, 1/lambda, e^{beta dt}, (e^{beta dt}-1)/beta
