@@ -45,6 +45,7 @@ extern "C" {
 #define TM_ERR_CUDA     (-2)   /* CUDA runtime error (context unusable)  */
 #define TM_ERR_NOMEM    (-3)   /* device or host allocation failed       */
 #define TM_ERR_STATE    (-4)   /* call not valid in the object's state   */
+#define TM_ERR_TIMEOUT  (-5)   /* a bounded device-side wait ran out     */
 
 /* per-instance status bits (OR-ed over all steps since the last reset) */
 #define TM_STATUS_NAN          0x1u  /* NaN or Inf produced               */
@@ -261,6 +262,46 @@ int tm_batch_power_spectrum(tm_batch* b, int k, int field, double binwidth, doub
 int tm_fke_advdiff_device(const void* dev_rho, const void* dev_gamma, const void* dev_vx, const void* dev_vy,
                           int precision, int L, double pref, double eps, const double* gD, int RD,
                           const double* gV, int RV, void* dev_out, void* stream);
+
+/* -- sweep surrogate: a small network trained on the integrator's own runs --
+ * No counterpart in the reference, which locates the critical point by
+ * uniform sweeps of the control parameter (critical_exp_delta,
+ * simulations/Percolation_FD/stochasticSPDP.cpp:1309-1422).  The surrogate
+ * maps features f = (a, log L, log t), affinely normalised by the caller, to two
+ * outputs (the caller's scaling of the mean density and the survival
+ * fraction) through
+ *     h1 = bf16(gelu(W1 f + b1)), h2 = bf16(gelu(W2 h1 + b2)),
+ *     h3 = gelu(W3 h2 + b3), y = W4 h3 + b4
+ * with 128 hidden units, gelu(x) = x/2 (1 + tanh(sqrt(2/pi)(x + 0.044715 x^3))),
+ * every weight matrix used as the BF16 rounding (nearest even) of its FP32
+ * master and all sums accumulated in FP32.  The two 128 x 128 layers and
+ * their backward GEMMs run on the tensor cores.
+ * Parameters: TM_MLP_NPARAMS floats W1[128][3] | b1[128] | W2[128][128] |
+ * b2[128] | W3[128][128] | b3[128] | W4[2][128] | b4[2] (row-major [out][in]).
+ * Loss: inv_norm * sum over samples of w0 (y0 - t0)^2 + w1 (y1 - t1)^2.  The
+ * backward pass rounds dz3 = (dy W4) * gelu'(.) and dz2 = (dz3 W3) * gelu'(.) to
+ * BF16 (the tensor-core operands); dz1 and all gradients stay FP32.  Partial
+ * gradients of 128-sample tiles are summed in tile order, so results are
+ * bit-reproducible.  The optimiser is full-batch Adam on the FP32 masters,
+ * with bias corrections 1/(1 - beta^t) computed on the host in double.
+ * tm_mlp_train returns TM_ERR_TIMEOUT if a bounded wait for a tensor-core
+ * operation ran out (the context stays usable). */
+#define TM_MLP_NPARAMS 33794
+typedef struct tm_mlp tm_mlp;
+int tm_mlp_create(tm_ctx* ctx, const float* params, tm_mlp** out);
+int tm_mlp_destroy(tm_mlp* m);
+/* replace the parameters; resets the Adam moments and step count */
+int tm_mlp_set_params(tm_mlp* m, const float* params);
+int tm_mlp_get_params(tm_mlp* m, float* params);
+/* the training set, copied to device memory: x n x 3, targets t n x 2, loss weights w n x 2 */
+int tm_mlp_set_data(tm_mlp* m, const float* x, const float* t, const float* w, int n);
+/* loss and gradient over the whole training set, no update (grad: TM_MLP_NPARAMS floats; either may be NULL) */
+int tm_mlp_loss_grad(tm_mlp* m, float inv_norm, double* loss, float* grad);
+/* `steps` full-batch Adam steps; loss_hist (optional, `steps` doubles) gets the loss before each update */
+int tm_mlp_train(tm_mlp* m, int steps, float lr, float beta1, float beta2, float eps, float inv_norm,
+                 double* loss_hist);
+/* y (n x 2) for features x (n x 3) */
+int tm_mlp_predict(tm_mlp* m, const float* x, int n, float* y);
 
 /* Packed-layout geometry without a batch (for callers that pack host buffers
  * before creating one): offsets[k] and the total, for nf fields per instance. */

@@ -11,7 +11,8 @@ import os
 PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "lib", "libtm.so")
 
-TM_OK, TM_ERR_INVALID, TM_ERR_CUDA, TM_ERR_NOMEM, TM_ERR_STATE = 0, -1, -2, -3, -4
+TM_OK, TM_ERR_INVALID, TM_ERR_CUDA, TM_ERR_NOMEM, TM_ERR_STATE, TM_ERR_TIMEOUT = 0, -1, -2, -3, -4, -5
+TM_MLP_NPARAMS = 33794
 TM_STATUS_NAN, TM_STATUS_NEGATIVE, TM_STATUS_SAMPLER_CAP = 0x1, 0x2, 0x4
 TM_FP64, TM_FP32 = 0, 1
 TM_REM_EULER_EXACT, TM_REM_RK4 = 0, 1
@@ -28,6 +29,8 @@ EXPORTS = (
     "tm_batch_set_launch", "tm_batch_get_launch", "tm_batch_autotune", "tm_run_dp", "tm_run_rietkerk",
     "tm_layout", "tm_observe_noalloc", "tm_power_spectrum_device", "tm_batch_power_spectrum",
     "tm_batch_set_site_coeff", "tm_batch_box_means", "tm_fke_advdiff_device",
+    "tm_mlp_create", "tm_mlp_destroy", "tm_mlp_set_params", "tm_mlp_get_params", "tm_mlp_set_data",
+    "tm_mlp_loss_grad", "tm_mlp_train", "tm_mlp_predict",
 )
 
 
@@ -66,6 +69,7 @@ def lib():
         L = C.CDLL(LIB_PATH)
         vp, i64, u32p, dp = C.c_void_p, C.c_int64, C.POINTER(C.c_uint32), C.POINTER(C.c_double)
         i64p = C.POINTER(C.c_int64)
+        fp = C.POINTER(C.c_float)
         sig = {
             "tm_abi_version": ([], C.c_int),
             "tm_error_string": ([C.c_int], C.c_char_p),
@@ -108,6 +112,14 @@ def lib():
             "tm_batch_box_means": ([vp, C.c_int, C.c_int, C.c_int, dp], C.c_int),
             "tm_fke_advdiff_device": ([vp, vp, vp, vp, C.c_int, C.c_int, C.c_double, C.c_double, dp, C.c_int, dp,
                                        C.c_int, vp, vp], C.c_int),
+            "tm_mlp_create": ([vp, fp, C.POINTER(vp)], C.c_int),
+            "tm_mlp_destroy": ([vp], C.c_int),
+            "tm_mlp_set_params": ([vp, fp], C.c_int),
+            "tm_mlp_get_params": ([vp, fp], C.c_int),
+            "tm_mlp_set_data": ([vp, fp, fp, fp, C.c_int], C.c_int),
+            "tm_mlp_loss_grad": ([vp, C.c_float, dp, fp], C.c_int),
+            "tm_mlp_train": ([vp, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, dp], C.c_int),
+            "tm_mlp_predict": ([vp, fp, C.c_int, fp], C.c_int),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)

@@ -22,7 +22,8 @@ OUT_DIR = os.path.join(PKG, "lib")
 OBJ_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT_DIR, "libtm.so")
 SWEEP = os.path.join(OUT_DIR, "tm_sweep")
-SOURCES = ["tm_step.cu", "tm_rk4.cu", "tm_measure.cu", "tm_capi.cu", "tm_noalloc.cu", "tm_spectrum.cu", "tm_fke.cu"]
+SOURCES = ["tm_step.cu", "tm_rk4.cu", "tm_measure.cu", "tm_capi.cu", "tm_noalloc.cu", "tm_spectrum.cu", "tm_fke.cu",
+           "tm_mlp.cu"]
 HEADERS = ["tm_device.cuh", "tm_kernels.cuh", "tm_zig_table.cuh", os.path.join("..", "..", "include", "tm.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",

@@ -399,6 +399,7 @@ const char* tm_error_string(int code)
     case TM_ERR_CUDA: return "CUDA runtime error";
     case TM_ERR_NOMEM: return "out of memory";
     case TM_ERR_STATE: return "invalid state for this call";
+    case TM_ERR_TIMEOUT: return "a bounded device wait ran out";
     default: return "unknown error";
     }
 }
