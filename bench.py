@@ -6,10 +6,16 @@ finite-size sweep of the DP Langevin model
     d rho = (a rho - b rho^2 + D Lap rho) dt + sigma sqrt(rho) dW,
     b = 2, D = 1, sigma = 1, dx = 1, dt = 0.1, Euler-exact remainder + Dornic draw,
 L in {64, 128, 256, 512, 1024} x 32 replicates x 16 a-values log-spaced within
-2 % of a = 0.72 (2560 instances, 714,604,544 sites), FP32 state with FP64
-reductions, rho0 = 1 + U(-0.01, 0.01) (seed 0): every site is live, so every
-site runs the full Poisson -> Gamma draw (the costly regime).  Synthetic inputs:
+2 % of the critical point a_c = 0.530 (2560 instances, 715,128,832 sites), FP32
+state with FP64 reductions, rho0 = 1 + U(-0.01, 0.01) (seed 0): every site is
+live, so every site runs the full Poisson -> Gamma draw (the costly regime).
+a_c is where the decay exponent of rho(t) crosses the 2-D DP value at
+L = 512-1024 (measured by trophic_maelstorm_gb300.surrogate).  Synthetic inputs:
 the reference ships no data for this path.
+
+The second half of the metric, the full runs needed to locate a_c to +-1e-3,
+is the `critical_point_search` extra: the surrogate-guided search against a
+uniform sweep of [0.50, 0.56] (a reduced corpus, L <= 256, to keep the run short).
 
 Metric: site-updates/s (one lattice site of one instance advanced one step).
 
@@ -38,7 +44,7 @@ sys.path.insert(0, REPO)
 LS = (64, 128, 256, 512, 1024)
 REPS = 32
 NA = 16
-A_CENTER = 0.72
+A_CENTER = 0.530          # measured critical point of b=2, D=1, sigma=1, dt=0.1
 MODEL = dict(b=2.0, D=1.0, sigma=1.0, dt=0.1, dx=1.0)
 BYTES_PER_SITE_FP32 = 8  # read rho, write rho (neighbours from registers/shuffles)
 METRIC = "site-updates/s at L=1024 (batched FP32 vs plain FP64); runs to locate a_c \u00b11e-3"
@@ -323,6 +329,23 @@ def rietkerk_4096(ctx, tmg, torch, args, steps=10, L=4096, precision=None):
             "kernels_per_step": 2}
 
 
+def critical_point_search(ctx):
+    """Full runs needed to locate a_c to +-1e-3: surrogate-guided (tensor-core MLP
+    trained on a corpus of integrator runs) against a uniform sweep, judged by
+    8 replicates at L = 256 to t = 1000."""
+    from trophic_maelstorm_gb300 import surrogate as sg
+    t0 = time.perf_counter()
+    r = sg.critical_point_study(ctx, Ls=(64, 128, 256), n_a=40, n_rep=15, judge_L=256, judge_rep=8,
+                                t_max=1000.0, t1=100.0, seed=1)
+    return {"runs_guided": r["guided"]["runs"], "runs_uniform": r["uniform"]["runs"],
+            "ratio": r["runs_ratio_uniform_over_guided"], "bracket_guided": r["guided"]["bracket"],
+            "bracket_uniform": r["uniform"]["bracket"], "a_hat": r["surrogate_a_hat"],
+            "corpus_runs": r["corpus"]["runs"], "corpus_site_updates_per_s":
+                r["corpus"]["site_updates"] / r["corpus"]["seconds"],
+            "fit_seconds": r["fit"]["seconds"], "fit_loss_last": r["fit"]["loss_last"],
+            "judge": r["judge"], "wall_s": time.perf_counter() - t0}
+
+
 def run_ours(args):
     import torch
     import trophic_maelstorm_gb300 as tmg
@@ -402,6 +425,7 @@ def run_ours(args):
         extras["plain_fp64_single_instance"] = plain_fp64(ctx, tmg, torch, args)
         extras["late_regime"] = late_regime(ctx, tmg, torch, args)
         extras["rietkerk_4096"] = rietkerk_4096(ctx, tmg, torch, args)
+        extras["critical_point_search"] = critical_point_search(ctx)
 
     hbm, peak_kind = peaks()
     avg_launch_s = statistics.mean(per) * 1e-3
@@ -421,7 +445,8 @@ def run_ours(args):
             "config": {"workload": "ragged DP Dornic sweep: L in {64..1024} x 32 replicates x 16 a (2560 instances)"
                        if args.workload == "sweep" else f"profiling case {args.workload}",
                        "sites_per_step": sites, "b": 2.0, "D": 1.0, "sigma": 1.0, "dt": 0.1,
-                       "a_values": "16 log-spaced in [0.7056, 0.7344]", "init": "1+U(-0.01,0.01), all sites live",
+                       "a_values": f"16 log-spaced in [{a_values()[0]:.4f}, {a_values()[-1]:.4f}]",
+                       "init": "1+U(-0.01,0.01), all sites live",
                        "state": "FP32, FP64 reductions", "l2": "inputs larger than L2 (2.86 GB state per buffer)",
                        "launch": {"rows_per_task": rows, "ctas_per_sm": ctas}, "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",

@@ -92,3 +92,17 @@ def test_training_is_reproducible_and_reduces_the_loss(env):
     assert np.array_equal(runs[0][0], runs[1][0])
     hist = runs[0][0]
     assert hist[-1] < 0.1 * hist[0]
+
+
+def test_guided_search_needs_fewer_full_runs(env):
+    """What the network gains: on a small judge (L = 128, 16 replicates, t <= 300)
+    the surrogate-guided bracket agrees with the uniform sweep's and needs at
+    least 4x fewer full simulations."""
+    tmg, sg, so, ctx = env
+    res = sg.critical_point_study(ctx, Ls=(64, 128), n_a=24, n_rep=8, judge_L=128, judge_rep=16, t_max=300.0,
+                                  t1=30.0, seed=3)
+    gb, ub = res["guided"]["bracket"], res["uniform"]["bracket"]
+    assert gb is not None and ub is not None
+    assert abs(sum(gb) / 2 - sum(ub) / 2) <= 4e-3
+    assert res["guided"]["runs"] * 4 <= res["uniform"]["runs"]
+    assert res["fit"]["loss_last"] < 0.05 * res["fit"]["loss_first"]
