@@ -329,6 +329,39 @@ def rietkerk_4096(ctx, tmg, torch, args, steps=10, L=4096, precision=None):
             "kernels_per_step": 2}
 
 
+def fke_advdiff_timing(ctx, L=1024, reps=5):
+    """The consumer-movement operator (advdiff_FKE_MultiSp) on one L x L FP64 field:
+    the GPU gather (tm_fke_advdiff_device, scratch allocation and synchronisation
+    included) against the oracle's CPU scatter in the reference's loop order
+    (one thread; this leg is a CPU baseline)."""
+    import torch
+    import trophic_maelstorm_gb300 as tmg
+    from oracle import oracle as o
+    rng = np.random.default_rng(5)
+    rho = rng.uniform(0, 2, (L, L))
+    rho[rng.random((L, L)) < 0.3] = 0.0
+    gam = rng.uniform(0, 1, (L, L))
+    vx = rng.uniform(-1, 1, (L, L))
+    vy = rng.uniform(-1, 1, (L, L))
+    p = tmg.fke_parameters(1.0, 1.0, 1.0, 1.5)
+    dev = torch.device("cuda", ctx.device)
+    ts = [torch.as_tensor(a, dtype=torch.float64, device=dev) for a in (rho, gam, vx, vy)]
+    tmg.fke_advdiff(*ts, p)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        out = tmg.fke_advdiff(*ts, p)
+    torch.cuda.synchronize(dev)
+    gpu_ms = (time.perf_counter() - t0) * 1e3 / reps
+    o.build()
+    t0 = time.perf_counter()
+    ref = o.fke_advdiff(rho, gam, vx, vy, p.pref, p.gD, p.gV)
+    cpu_ms = (time.perf_counter() - t0) * 1e3
+    err = float(np.abs(out.cpu().numpy().reshape(-1) - ref).max() / np.abs(ref).max())
+    return {"L": L, "RD": p.RD, "RV": p.RV, "gpu_ms": gpu_ms, "cpu_baseline_ms": cpu_ms, "cpu_threads": 1,
+            "cpu_kind": "port (reference loop order)", "max_rel_diff": err}
+
+
 def critical_point_search(ctx):
     """Full runs needed to locate a_c to +-1e-3: surrogate-guided (tensor-core MLP
     trained on a corpus of integrator runs) against a uniform sweep, judged by
@@ -426,6 +459,7 @@ def run_ours(args):
         extras["late_regime"] = late_regime(ctx, tmg, torch, args)
         extras["rietkerk_4096"] = rietkerk_4096(ctx, tmg, torch, args)
         extras["critical_point_search"] = critical_point_search(ctx)
+        extras["fke_advdiff"] = fke_advdiff_timing(ctx)
 
     hbm, peak_kind = peaks()
     avg_launch_s = statistics.mean(per) * 1e-3
