@@ -289,3 +289,15 @@ def test_reference_rows_shape(tmg, ctx):
     assert rows.shape == (11 + 3, 8)
     assert np.allclose(rows[:, 0], 0.72) and np.allclose(rows[:, 1], 8)
     assert rows[0, 3] == pytest.approx(1.0) and rows[0, 5] == 8
+
+
+def test_fp32_state_is_statistically_equivalent_to_fp64(tmg, ctx):
+    """FP32 field state against FP64 near the critical point (same seeds): the
+    ensemble mean density and survival agree within 3.5 combined standard errors and
+    the replicate spatial means pass KS at p > 0.01 / n_t at every time."""
+    from trophic_maelstorm_gb300 import study
+    r = study.dp_precision_study(L=64, n_rep=96, a=0.53, t_max=100.0, seed=11)
+    n_t = len(r["t"])
+    assert r["status"] == [0, 0]
+    assert r["max_abs_z_rho"] < 3.5 and r["max_abs_z_surv"] < 3.5
+    assert r["min_ks_p"] > 0.01 / n_t
