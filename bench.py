@@ -187,6 +187,16 @@ def cpu_baseline(threads, budget_s=15.0):
                       f"{el:.1f} s, OpenMP over instances"}
 
 
+def workload_config(kind):
+    """The config block both arms print for a workload."""
+    return {"workload": "ragged DP Dornic sweep: L in {64..1024} x 32 replicates x 16 a (2560 instances)"
+            if kind == "sweep" else f"profiling case {kind}",
+            "sites_per_step": int(sum(L * L for L in workload(kind)[0])), "b": 2.0, "D": 1.0, "sigma": 1.0,
+            "dt": 0.1, "a_values": f"16 log-spaced in [{a_values()[0]:.4f}, {a_values()[-1]:.4f}]",
+            "init": "1+U(-0.01,0.01), all sites live", "state": "FP32, FP64 reductions",
+            "l2": "inputs larger than L2 (2.86 GB state per buffer)"}
+
+
 def run_reference(args):
     rank, world, _ = dist_setup(args.gpus)
     if rank != 0:
@@ -212,10 +222,10 @@ def run_reference(args):
         "unit": "site-updates/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "DP Dornic sweep, L=1024 subset sample", "instances": n_inst, "L": 1024,
-                   "b": 2.0, "D": 1.0, "sigma": 1.0, "dt": 0.1, "init": "1+U(-0.01,0.01)"},
+        "config": dict(workload_config(args.workload), parallelism=f"host threads x{threads}"),
         "cpu_baseline": {"value": val, "unit": "site-updates/s", "cores": threads, "kind": "port",
-                         "sample": f"{n_inst} L=1024 instances x {args.steps} steps per timed run"},
+                         "sample": f"each step: {n_inst} L=1024 instances of the workload (a cycling over its 16 "
+                                   f"values), {args.steps} timed steps, OpenMP over instances"},
         "e2e": {"value": val, "unit": "site-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -476,13 +486,8 @@ def run_ours(args):
             "value": value, "unit": "site-updates/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "ragged DP Dornic sweep: L in {64..1024} x 32 replicates x 16 a (2560 instances)"
-                       if args.workload == "sweep" else f"profiling case {args.workload}",
-                       "sites_per_step": sites, "b": 2.0, "D": 1.0, "sigma": 1.0, "dt": 0.1,
-                       "a_values": f"16 log-spaced in [{a_values()[0]:.4f}, {a_values()[-1]:.4f}]",
-                       "init": "1+U(-0.01,0.01), all sites live",
-                       "state": "FP32, FP64 reductions", "l2": "inputs larger than L2 (2.86 GB state per buffer)",
-                       "launch": {"rows_per_task": rows, "ctas_per_sm": ctas}, "parallelism": f"replicas x{world}"},
+            "config": dict(workload_config(args.workload), launch={"rows_per_task": rows, "ctas_per_sm": ctas},
+                           parallelism=f"replicas x{world}"),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
                          "kernel": "dornic_step_kernel<float, euler>", "alg_bytes_per_site": BYTES_PER_SITE_FP32,
