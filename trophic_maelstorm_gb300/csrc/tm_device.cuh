@@ -11,7 +11,10 @@
 //   Philox4x32-10  Salmon, Moraes, Dror, Shaw, SC'11 ("as easy as 1, 2, 3")
 //   Poisson m>=32  Hormann 1993, PTRS (transformed rejection with squeeze)
 //   Poisson m<32   inversion from the top of the tail with one 32-bit word
-//   Gamma          Marsaglia & Tsang 2000, with the U^(1/k) boost for k<1
+//   Gamma          Marsaglia & Tsang 2000, with the U^(1/k) boost for k<1 and
+//                  the squeeze (1-u) 108 d min(1, 1+cx) > x^4: the acceptance
+//                  bound is 3d h(cx), h(y) = log(1+y) - y + y^2/2 - y^3/3 >=
+//                  -y^4 / (4 min(1, 1+y)), and log u <= u - 1
 //   normal         ziggurat (Marsaglia & Tsang 2000), tables from oracle/gen_ziggurat.py
 //   log / exp      Cody-Waite argument reduction + Taylor series
 // The reference draws the same two distributions from libstdc++
@@ -469,10 +472,11 @@ __device__ __forceinline__ T gamma_mt(Stream<T>& g, T k, const SmemTab<T>& tb)
             if (v > T(0)) { ok = true; break; }
         }
         if (!ok) break;
+        const T mm = (v < T(1)) ? v : T(1);
         v = (v * v) * v;
         const T u = g.open();
         const T x2 = x * x;
-        if (u < T(1) - T(0.0331) * (x2 * x2)) { res = d * v; done = true; break; }
+        if ((T(1) - u) * ((T(108) * d) * mm) > x2 * x2) { res = d * v; done = true; break; }
         if (tm_log_pos(u) < T(0.5) * x2 + d * ((T(1) - v) + tm_log(v))) { res = d * v; done = true; break; }
     }
     if (!done) g.status |= TM_STATUS_CAP_BIT;
@@ -583,10 +587,11 @@ __device__ __forceinline__ float dornic_draw_fast(uint64_t seed, uint32_t site, 
     const float x = (float)hz * tb.zw[iz];
     float v = 1.0f + c * x;
     if (!(v > 0.0f)) { deferred = true; return 0.0f; }
+    const float mm = (v < 1.0f) ? v : 1.0f;
     v = (v * v) * v;
     const float u = ((float)(wu >> 8) + 0.5f) * 0x1p-24f;
     const float x2 = x * x;
-    if (!(u < 1.0f - 0.0331f * (x2 * x2))) { deferred = true; return 0.0f; }
+    if (!((1.0f - u) * ((108.0f * d) * mm) > x2 * x2)) { deferred = true; return 0.0f; }
     float res = d * v;
     if (boost) {
         const float ub = ((float)(wb >> 8) + 0.5f) * 0x1p-24f;
