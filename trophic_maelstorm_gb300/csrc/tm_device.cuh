@@ -528,6 +528,7 @@ __device__ __forceinline__ T dornic_draw(Stream<T>& g, T m, T mu1, T inv_lambda,
 // dornic_draw's bit for bit; otherwise (*deferred) the caller recomputes the
 // site with dornic_draw.
 constexpr int kFastInv = 24;
+static_assert(kFastInv % 4 == 0, "the inversion takes four terms per trip");
 
 __device__ __forceinline__ float dornic_draw_fast(uint64_t seed, uint32_t site, int64_t step, float m, float mu1,
                                                   float inv_lambda, int sampler, const SmemTab<float>& tb,
@@ -563,14 +564,26 @@ __device__ __forceinline__ float dornic_draw_fast(uint64_t seed, uint32_t site, 
         float p = small ? 0.0f : tm_exp(-m);
         float q = small ? tm_negexpm1(m) : 1.0f - p;
         if (small && u < q) p = tm_exp(-m);
+        // four terms per trip: the same products and differences as one term
+        // per trip (kFastInv is a multiple of 4), with a quarter of the loop
+        // control and the table loads issued together
         int it = 0;
         while (u < q && it < kFastInv) {
-            ++it;
-            n = n + 1.0f;
-            p = (p * m) * tb.rcp[it];
-            q = q - p;
+            const float p1 = (p * m) * tb.rcp[it + 1];
+            const float q1 = q - p1;
+            if (!(u < q1)) { it += 1; q = q1; break; }
+            const float p2 = (p1 * m) * tb.rcp[it + 2];
+            const float q2 = q1 - p2;
+            if (!(u < q2)) { it += 2; q = q2; break; }
+            const float p3 = (p2 * m) * tb.rcp[it + 3];
+            const float q3 = q2 - p3;
+            if (!(u < q3)) { it += 3; q = q3; break; }
+            p = (p3 * m) * tb.rcp[it + 4];
+            q = q3 - p;
+            it += 4;
         }
         if (u < q) { deferred = true; return 0.0f; }
+        n = (float)it;
     }
     const float k = mu1 + n;
     if (!(k > 0.0f)) return 0.0f;  // Gamma(0) = 0, no draw
