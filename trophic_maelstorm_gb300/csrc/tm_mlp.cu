@@ -2,9 +2,12 @@
 // weights, trained and evaluated on the 5th-generation tensor cores.
 //
 // The reference has no learned part; the network, its rounding points and its
-// optimiser are specified in include/tm.h (tm_mlp_*).  One CTA of 128 threads
-// owns a tile of 128 samples (thread t = sample t = TMEM lane t) and runs the
-// whole forward and backward pass of that tile:
+// optimiser are specified in include/tm.h (tm_mlp_*).  One CTA owns a tile of
+// 128 samples (sample t = TMEM lane t) and runs the whole forward and backward
+// pass of that tile with 16 warps: warp w reads TMEM lane quarter w % 4 (the
+// quarter a warp may access) and handles column slice w / 4, so a thread does
+// 32 of the 128 columns of its sample and the 128-sample column sums are split
+// four ways:
 //   * the two 128x128 layers and the four GEMMs of their backward pass are
 //     tcgen05.mma (kind::f16, BF16 x BF16 -> FP32, M = N = K = 128), issued by
 //     one thread, with both operands in shared memory in the K-major
@@ -29,7 +32,9 @@
 
 namespace {
 
-constexpr int NT = 128;              // threads per CTA = samples per tile = TMEM lanes
+constexpr int TS = 128;              // samples per tile = TMEM lanes
+constexpr int NT = 512;              // threads per CTA: 4 column slices x 128 samples
+constexpr int NS = NT / TS;          // column slices (32 columns each)
 constexpr int OFF_W1 = 0, OFF_B1 = 384, OFF_W2 = 512, OFF_B2 = 16896, OFF_W3 = 17024, OFF_B3 = 33408,
               OFF_W4 = 33536, OFF_B4 = 33792, NP = 33794;
 static_assert(NP == TM_MLP_NPARAMS, "parameter layout");
@@ -44,11 +49,12 @@ constexpr int SM_B4 = SM_W4 + 1024;
 constexpr int SM_X = SM_B4 + 16;
 constexpr int SM_DY = SM_X + 1536;
 constexpr int SM_LOSS = SM_DY + 1024;
-constexpr int SM_BAR = SM_LOSS + 512;
+constexpr int SM_RED = SM_LOSS + 512;       // [NS][128][3] FP32 partial sums
+constexpr int SM_BAR = SM_RED + NS * TS * 3 * 4;
 constexpr int SM_TMEM = SM_BAR + 8;
 constexpr int SM_TOTAL = SM_TMEM + 8;
 constexpr int FPAD = 129;            // row stride (floats) of the FP32 column-sum scratch over buffers 0-2
-static_assert(NT * FPAD * 4 <= 3 * BUF, "scratch fits buffers 0-2");
+static_assert(TS * FPAD * 4 <= 3 * BUF, "scratch fits buffers 0-2");
 static_assert(SM_BAR % 8 == 0, "mbarrier alignment");
 
 constexpr int kWaitLimit = 1 << 22;  // polls of an MMA completion before the CTA gives up (~0.3 s)
@@ -154,11 +160,11 @@ __device__ __forceinline__ void load_tile(unsigned char* dst, const __nv_bfloat1
     for (int c = threadIdx.x; c < 2048; c += NT) *reinterpret_cast<uint4*>(dst + cm(c >> 4, (c & 15) * 8)) = s[c];
 }
 
-// sum over k of row r of a K-major BF16 tile, k ascending
-__device__ __forceinline__ float row_sum(const unsigned char* buf, int r)
+// sum over k in [32 p, 32 p + 32) of row r of a K-major BF16 tile, k ascending
+__device__ __forceinline__ float row_sum_part(const unsigned char* buf, int r, int p)
 {
     float s = 0.0f;
-    for (int g = 0; g < 16; ++g) {
+    for (int g = 4 * p; g < 4 * p + 4; ++g) {
         const uint4 q = *reinterpret_cast<const uint4*>(buf + cm(r, g * 8));
         const __nv_bfloat16* h = reinterpret_cast<const __nv_bfloat16*>(&q);
 #pragma unroll
@@ -209,35 +215,41 @@ __global__ void __launch_bounds__(NT, 1) mlp_tile_kernel(MlpArgs a)
     float* xs = reinterpret_cast<float*>(sm + SM_X);
     float* dys = reinterpret_cast<float*>(sm + SM_DY);
     float* ls = reinterpret_cast<float*>(sm + SM_LOSS);
+    float* red = reinterpret_cast<float*>(sm + SM_RED);    // [NS][TS][3]
     uint64_t* bar = reinterpret_cast<uint64_t*>(sm + SM_BAR);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + SM_TMEM);
 
-    const int t = threadIdx.x, warp = t >> 5;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int q = warp & 3, cs = warp >> 2;            // TMEM lane quarter, column slice
+    const int t = q * 32 + (tid & 31);                 // this thread's sample (= TMEM lane)
+    const int c0 = cs * 32;                            // first column of this thread's slice
     const int tile = blockIdx.x;
-    const long long s = (long long)tile * NT + t;
+    const long long s = (long long)tile * TS + t;
     const bool valid = s < a.n;
     const uint32_t bar_a = saddr(bar);
 
-    for (int i = t; i < 384; i += NT) W1s[i] = bf16r(a.p[OFF_W1 + i]);
-    for (int i = t; i < 128; i += NT) {
+    for (int i = tid; i < 384; i += NT) W1s[i] = bf16r(a.p[OFF_W1 + i]);
+    for (int i = tid; i < 128; i += NT) {
         bs[i] = a.p[OFF_B1 + i];
         bs[128 + i] = a.p[OFF_B2 + i];
         bs[256 + i] = a.p[OFF_B3 + i];
     }
-    for (int i = t; i < 256; i += NT) W4s[i] = bf16r(a.p[OFF_W4 + i]);
-    if (t < 2) b4s[t] = a.p[OFF_B4 + t];
+    for (int i = tid; i < 256; i += NT) W4s[i] = bf16r(a.p[OFF_W4 + i]);
+    if (tid < 2) b4s[tid] = a.p[OFF_B4 + tid];
     float x0 = 0.0f, x1 = 0.0f, x2 = 0.0f;
     if (valid) {
         x0 = a.x[3 * s];
         x1 = a.x[3 * s + 1];
         x2 = a.x[3 * s + 2];
     }
-    xs[3 * t] = x0;
-    xs[3 * t + 1] = x1;
-    xs[3 * t + 2] = x2;
+    if (cs == 0) {
+        xs[3 * t] = x0;
+        xs[3 * t + 1] = x1;
+        xs[3 * t + 2] = x2;
+    }
     load_tile(B0, a.W2);
     load_tile(B1, a.W3);
-    if (t == 0) {
+    if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(bar_a) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -250,7 +262,7 @@ __global__ void __launch_bounds__(NT, 1) mlp_tile_kernel(MlpArgs a)
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tslot;
-    const uint32_t lane = tmem + ((uint32_t)(warp * 32) << 16);   // this warp's 32 TMEM lanes
+    const uint32_t lane = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;   // this warp's lanes and slice
     float* gp = TRAIN ? a.grad_part + (size_t)tile * PS : nullptr;
     uint32_t phase = 0;
     bool failed = false;
@@ -259,19 +271,20 @@ __global__ void __launch_bounds__(NT, 1) mlp_tile_kernel(MlpArgs a)
 
     do {
         // ---- layer 1 (CUDA cores): h1 = bf16(gelu(W1 x + b1)) -> B2 (A operand); h1^T -> B3
-        for (int jc = 0; jc < 16; ++jc) {
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                const int j = jc * 8 + q;
+        for (int g = 0; g < 4; ++g) {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const int j = c0 + g * 8 + i;
                 const float z = ((W1s[3 * j] * x0 + W1s[3 * j + 1] * x1) + W1s[3 * j + 2] * x2) + bs[j];
-                hb[q] = __float2bfloat16_rn(gelu(z));
-                if (TRAIN) store1(B3, j, t, hb[q]);
+                hb[i] = __float2bfloat16_rn(gelu(z));
+                if (TRAIN) store1(B3, j, t, hb[i]);
             }
-            store8(B2, t, jc * 8, hb);
+            store8(B2, t, c0 + g * 8, hb);
         }
         fence_async_smem();
         __syncthreads();
-        if (t == 0) {
+        if (tid == 0) {
             tc_fence_after();
             mma_128(tmem + 0, saddr(B2), saddr(B0));          // a2 - b2 -> TMEM cols 0..127
             mma_commit(bar_a);
@@ -282,22 +295,21 @@ __global__ void __launch_bounds__(NT, 1) mlp_tile_kernel(MlpArgs a)
         tc_fence_after();
 
         // ---- layer 2 epilogue: h2 = bf16(gelu(a2)) -> B2 (A operand); h2^T -> B4
-        for (int c = 0; c < 4; ++c) {
-            tmem_ld32(lane + c * 32, v);
-            for (int g = 0; g < 4; ++g) {
+        tmem_ld32(lane + 0, v);
 #pragma unroll
-                for (int q = 0; q < 8; ++q) {
-                    const int j = c * 32 + g * 8 + q;
-                    hb[q] = __float2bfloat16_rn(gelu(v[g * 8 + q] + bs[128 + j]));
-                    if (TRAIN) store1(B4, j, t, hb[q]);
-                }
-                store8(B2, t, c * 32 + g * 8, hb);
+        for (int g = 0; g < 4; ++g) {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const int j = c0 + g * 8 + i;
+                hb[i] = __float2bfloat16_rn(gelu(v[g * 8 + i] + bs[128 + j]));
+                if (TRAIN) store1(B4, j, t, hb[i]);
             }
+            store8(B2, t, c0 + g * 8, hb);
         }
         fence_async_smem();
         tc_fence_before();
         __syncthreads();
-        if (t == 0) {
+        if (tid == 0) {
             tc_fence_after();
             mma_128(tmem + 128, saddr(B2), saddr(B1));        // a3 - b3 -> TMEM cols 128..255
             mma_commit(bar_a);
@@ -307,167 +319,212 @@ __global__ void __launch_bounds__(NT, 1) mlp_tile_kernel(MlpArgs a)
         if (failed) break;
         tc_fence_after();
 
-        // ---- layer 3 epilogue and output layer: y = W4 gelu(a3) + b4 (h3 kept FP32 in F for dW4)
-        float y0 = 0.0f, y1 = 0.0f;
-        for (int c = 0; c < 4; ++c) {
-            tmem_ld32(lane + 128 + c * 32, v);
+        // ---- layer 3 epilogue and output layer: y = W4 gelu(a3) + b4, slice partials summed in
+        //      slice order (h3 kept FP32 in F for dW4)
+        {
+            float y0 = 0.0f, y1 = 0.0f;
+            tmem_ld32(lane + 128, v);
 #pragma unroll
             for (int i = 0; i < 32; ++i) {
-                const int j = c * 32 + i;
+                const int j = c0 + i;
                 const float h = gelu(v[i] + bs[256 + j]);
                 y0 = y0 + W4s[j] * h;
                 y1 = y1 + W4s[128 + j] * h;
                 if (TRAIN) F[j * FPAD + t] = h;
             }
+            red[(cs * TS + t) * 3] = y0;
+            red[(cs * TS + t) * 3 + 1] = y1;
         }
-        y0 = y0 + b4s[0];
-        y1 = y1 + b4s[1];
-        if (!TRAIN) {
-            if (valid) {
-                a.y_out[2 * s] = y0;
-                a.y_out[2 * s + 1] = y1;
-            }
-            break;
-        }
-
-        // ---- loss and output-layer gradients
-        float e0 = 0.0f, e1 = 0.0f, w0 = 0.0f, w1 = 0.0f;
-        if (valid) {
-            e0 = y0 - a.y[2 * s];
-            e1 = y1 - a.y[2 * s + 1];
-            w0 = a.w[2 * s];
-            w1 = a.w[2 * s + 1];
-        }
-        ls[t] = w0 * e0 * e0 + w1 * e1 * e1;
-        const float dy0 = ((2.0f * w0) * e0) * a.inv_norm;
-        const float dy1 = ((2.0f * w1) * e1) * a.inv_norm;
-        dys[2 * t] = dy0;
-        dys[2 * t + 1] = dy1;
         __syncthreads();
+        float dy0 = 0.0f, dy1 = 0.0f;
+        if (cs == 0) {
+            float y0 = 0.0f, y1 = 0.0f;
+            for (int p = 0; p < NS; ++p) {
+                y0 = y0 + red[(p * TS + t) * 3];
+                y1 = y1 + red[(p * TS + t) * 3 + 1];
+            }
+            y0 = y0 + b4s[0];
+            y1 = y1 + b4s[1];
+            if (!TRAIN) {
+                if (valid) {
+                    a.y_out[2 * s] = y0;
+                    a.y_out[2 * s + 1] = y1;
+                }
+            } else {
+                // loss and output-layer gradient of this sample
+                float e0 = 0.0f, e1 = 0.0f, w0 = 0.0f, w1 = 0.0f;
+                if (valid) {
+                    e0 = y0 - a.y[2 * s];
+                    e1 = y1 - a.y[2 * s + 1];
+                    w0 = a.w[2 * s];
+                    w1 = a.w[2 * s + 1];
+                }
+                ls[t] = w0 * e0 * e0 + w1 * e1 * e1;
+                dys[2 * t] = ((2.0f * w0) * e0) * a.inv_norm;
+                dys[2 * t + 1] = ((2.0f * w1) * e1) * a.inv_norm;
+            }
+        }
+        if (!TRAIN) break;
+        __syncthreads();
+        dy0 = dys[2 * t];
+        dy1 = dys[2 * t + 1];
         {
+            // gW4[o][j] = sum_u dy_o[u] h3[u][j]: thread (j = tid & 127, part p = tid >> 7) sums 32 samples
+            const int j = tid & 127, p = tid >> 7;
             float g0 = 0.0f, g1 = 0.0f;
-            for (int u = 0; u < NT; ++u) {
-                const float h = F[t * FPAD + u];
+            for (int u = 32 * p; u < 32 * p + 32; ++u) {
+                const float h = F[j * FPAD + u];
                 g0 = g0 + dys[2 * u] * h;
                 g1 = g1 + dys[2 * u + 1] * h;
             }
-            gp[OFF_W4 + t] = g0;
-            gp[OFF_W4 + 128 + t] = g1;
-            if (t == 0) {
-                float s0 = 0.0f, s1 = 0.0f, sl = 0.0f;
-                for (int u = 0; u < NT; ++u) {
-                    s0 = s0 + dys[2 * u];
-                    s1 = s1 + dys[2 * u + 1];
-                    sl = sl + ls[u];
-                }
-                gp[OFF_B4] = s0;
-                gp[OFF_B4 + 1] = s1;
-                a.loss_part[tile] = sl * a.inv_norm;
-            }
+            red[(p * TS + j) * 3] = g0;
+            red[(p * TS + j) * 3 + 1] = g1;
         }
-        __syncthreads();                                      // F (B0..B2) free again
+        __syncthreads();
+        if (tid < 128) {
+            float g0 = 0.0f, g1 = 0.0f;
+            for (int p = 0; p < NS; ++p) {
+                g0 = g0 + red[(p * TS + tid) * 3];
+                g1 = g1 + red[(p * TS + tid) * 3 + 1];
+            }
+            gp[OFF_W4 + tid] = g0;
+            gp[OFF_W4 + 128 + tid] = g1;
+        }
+        if (tid == 0) {
+            float s0 = 0.0f, s1 = 0.0f, sl = 0.0f;
+            for (int u = 0; u < TS; ++u) {
+                s0 = s0 + dys[2 * u];
+                s1 = s1 + dys[2 * u + 1];
+                sl = sl + ls[u];
+            }
+            gp[OFF_B4] = s0;
+            gp[OFF_B4 + 1] = s1;
+            a.loss_part[tile] = sl * a.inv_norm;
+        }
+        __syncthreads();                                      // F (B0..B2) and red free again
 
         // ---- dz3 = bf16((dy W4) * gelu'(a3)) -> B2 (A operand of dH2); dz3^T -> B5 (A operand of dW3)
         load_tile(B1, a.W3T);
-        for (int c = 0; c < 4; ++c) {
-            tmem_ld32(lane + 128 + c * 32, v);
-            for (int g = 0; g < 4; ++g) {
+        tmem_ld32(lane + 128, v);
 #pragma unroll
-                for (int q = 0; q < 8; ++q) {
-                    const int j = c * 32 + g * 8 + q;
-                    const float dh = dy0 * W4s[j] + dy1 * W4s[128 + j];
-                    hb[q] = __float2bfloat16_rn(dh * gelu_grad(v[g * 8 + q] + bs[256 + j]));
-                    store1(B5, j, t, hb[q]);
-                }
-                store8(B2, t, c * 32 + g * 8, hb);
+        for (int g = 0; g < 4; ++g) {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const int j = c0 + g * 8 + i;
+                const float dh = dy0 * W4s[j] + dy1 * W4s[128 + j];
+                hb[i] = __float2bfloat16_rn(dh * gelu_grad(v[g * 8 + i] + bs[256 + j]));
+                store1(B5, j, t, hb[i]);
             }
+            store8(B2, t, c0 + g * 8, hb);
         }
         fence_async_smem();
         tc_fence_before();
         __syncthreads();
-        if (t == 0) {
+        if (tid == 0) {
             tc_fence_after();
             mma_128(tmem + 256, saddr(B2), saddr(B1));        // dH2 = dz3 W3      -> cols 256..383
             mma_128(tmem + 384, saddr(B5), saddr(B4));        // gW3 = dz3^T h2    -> cols 384..511
             mma_commit(bar_a);
         }
-        gp[OFF_B3 + t] = row_sum(B5, t);
+        red[(cs * TS + t) * 3 + 2] = row_sum_part(B5, t, cs);   // gb3 partial: row t of dz3^T, samples 32 cs..
         failed = __syncthreads_or(!bar_wait(bar_a, phase));
         phase ^= 1;
         if (failed) break;
         tc_fence_after();
+        if (tid < 128) {
+            float sb = 0.0f;
+            for (int p = 0; p < NS; ++p) sb = sb + red[(p * TS + tid) * 3 + 2];
+            gp[OFF_B3 + tid] = sb;
+        }
 
         // ---- gW3 rows; dz2 = bf16(dH2 * gelu'(a2)) -> B2; dz2^T -> B5
         load_tile(B0, a.W2T);
-        for (int c = 0; c < 4; ++c) {
-            tmem_ld32(lane + 384 + c * 32, v);
-            float4* dst = reinterpret_cast<float4*>(gp + OFF_W3 + t * 128 + c * 32);
+        tmem_ld32(lane + 384, v);
+        {
+            float4* dst = reinterpret_cast<float4*>(gp + OFF_W3 + t * 128 + c0);
 #pragma unroll
             for (int i = 0; i < 8; ++i) dst[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
         }
-        for (int c = 0; c < 4; ++c) {
+        {
             float z[32];
-            tmem_ld32(lane + 256 + c * 32, v);
-            tmem_ld32(lane + 0 + c * 32, z);
-            for (int g = 0; g < 4; ++g) {
+            tmem_ld32(lane + 256, v);
+            tmem_ld32(lane + 0, z);
+    #pragma unroll
+        for (int g = 0; g < 4; ++g) {
 #pragma unroll
-                for (int q = 0; q < 8; ++q) {
-                    const int j = c * 32 + g * 8 + q;
-                    hb[q] = __float2bfloat16_rn(v[g * 8 + q] * gelu_grad(z[g * 8 + q] + bs[128 + j]));
-                    store1(B5, j, t, hb[q]);
+                for (int i = 0; i < 8; ++i) {
+                    const int j = c0 + g * 8 + i;
+                    hb[i] = __float2bfloat16_rn(v[g * 8 + i] * gelu_grad(z[g * 8 + i] + bs[128 + j]));
+                    store1(B5, j, t, hb[i]);
                 }
-                store8(B2, t, c * 32 + g * 8, hb);
+                store8(B2, t, c0 + g * 8, hb);
             }
         }
         fence_async_smem();
         tc_fence_before();
-        __syncthreads();
-        if (t == 0) {
+        __syncthreads();                                      // also: every gb3 read of red is done
+        if (tid == 0) {
             tc_fence_after();
             mma_128(tmem + 128, saddr(B2), saddr(B0));        // dH1 = dz2 W2      -> cols 128..255
             mma_128(tmem + 0, saddr(B5), saddr(B3));          // gW2 = dz2^T h1    -> cols 0..127
             mma_commit(bar_a);
         }
-        gp[OFF_B2 + t] = row_sum(B5, t);
+        red[(cs * TS + t) * 3 + 2] = row_sum_part(B5, t, cs);   // gb2 partial
         failed = __syncthreads_or(!bar_wait(bar_a, phase));
         phase ^= 1;
         if (failed) break;
         tc_fence_after();
+        if (tid < 128) {
+            float sb = 0.0f;
+            for (int p = 0; p < NS; ++p) sb = sb + red[(p * TS + tid) * 3 + 2];
+            gp[OFF_B2 + tid] = sb;
+        }
 
         // ---- gW2 rows; dz1 = dH1 * gelu'(z1) (FP32) -> F; gW1, gb1 by column sums
-        for (int c = 0; c < 4; ++c) {
-            tmem_ld32(lane + 0 + c * 32, v);
-            float4* dst = reinterpret_cast<float4*>(gp + OFF_W2 + t * 128 + c * 32);
+        tmem_ld32(lane + 0, v);
+        {
+            float4* dst = reinterpret_cast<float4*>(gp + OFF_W2 + t * 128 + c0);
 #pragma unroll
             for (int i = 0; i < 8; ++i) dst[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
         }
-        for (int c = 0; c < 4; ++c) {
-            tmem_ld32(lane + 128 + c * 32, v);
+        tmem_ld32(lane + 128, v);
 #pragma unroll
-            for (int i = 0; i < 32; ++i) {
-                const int j = c * 32 + i;
-                const float z = ((W1s[3 * j] * x0 + W1s[3 * j + 1] * x1) + W1s[3 * j + 2] * x2) + bs[j];
-                F[j * FPAD + t] = v[i] * gelu_grad(z);
-            }
+        for (int i = 0; i < 32; ++i) {
+            const int j = c0 + i;
+            const float z = ((W1s[3 * j] * x0 + W1s[3 * j + 1] * x1) + W1s[3 * j + 2] * x2) + bs[j];
+            F[j * FPAD + t] = v[i] * gelu_grad(z);
         }
-        __syncthreads();
+        __syncthreads();                                      // F complete; every gb2 read of red is done
         {
-            float g0 = 0.0f, g1 = 0.0f, g2 = 0.0f, gb = 0.0f;
-            for (int u = 0; u < NT; ++u) {
-                const float d = F[t * FPAD + u];
+            const int j = tid & 127, p = tid >> 7;
+            float g0 = 0.0f, g1 = 0.0f, g2 = 0.0f;
+            for (int u = 32 * p; u < 32 * p + 32; ++u) {
+                const float d = F[j * FPAD + u];
                 g0 = g0 + d * xs[3 * u];
                 g1 = g1 + d * xs[3 * u + 1];
                 g2 = g2 + d * xs[3 * u + 2];
-                gb = gb + d;
             }
-            gp[OFF_W1 + 3 * t] = g0;
-            gp[OFF_W1 + 3 * t + 1] = g1;
-            gp[OFF_W1 + 3 * t + 2] = g2;
-            gp[OFF_B1 + t] = gb;
+            red[(p * TS + j) * 3] = g0;
+            red[(p * TS + j) * 3 + 1] = g1;
+            red[(p * TS + j) * 3 + 2] = g2;
+        }
+        __syncthreads();
+        if (tid < 128) {
+            float g0 = 0.0f, g1 = 0.0f, g2 = 0.0f, gb = 0.0f;
+            for (int p = 0; p < NS; ++p) {
+                g0 = g0 + red[(p * TS + tid) * 3];
+                g1 = g1 + red[(p * TS + tid) * 3 + 1];
+                g2 = g2 + red[(p * TS + tid) * 3 + 2];
+            }
+            for (int u = 0; u < TS; ++u) gb = gb + F[tid * FPAD + u];
+            gp[OFF_W1 + 3 * tid] = g0;
+            gp[OFF_W1 + 3 * tid + 1] = g1;
+            gp[OFF_W1 + 3 * tid + 2] = g2;
+            gp[OFF_B1 + tid] = gb;
         }
     } while (false);
 
-    if (failed && t == 0) atomicExch(a.err, 1);
+    if (failed && tid == 0) atomicExch(a.err, 1);
     tc_fence_before();
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" :: "r"(tmem) : "memory");
@@ -735,7 +792,7 @@ int tm_mlp_set_data(tm_mlp* m, const float* x, const float* y, const float* w, i
             return TM_ERR_NOMEM;
         }
     }
-    const int rc = grow_tiles(m, (n + NT - 1) / NT);
+    const int rc = grow_tiles(m, (n + TS - 1) / TS);
     if (rc != TM_OK) return rc;
     cudaStream_t s = m->ctx->stream;
     MLP_CUDA(cudaMemcpyAsync(m->x, x, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, s));
@@ -755,7 +812,7 @@ int tm_mlp_loss_grad(tm_mlp* m, float inv_norm, double* loss, float* grad)
         m->loss_cap = 64;
     }
     cudaStream_t s = m->ctx->stream;
-    const int tiles = (m->n + NT - 1) / NT;
+    const int tiles = (m->n + TS - 1) / TS;
     mlp_tile_kernel<true><<<tiles, NT, SM_TOTAL, s>>>(tile_args(m, m->x, m->n, inv_norm, nullptr));
     AdamArgs a = adam_args(m, tiles, m->loss_dev, m->grad, 0, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f);
     mlp_adam_kernel<<<(NP + 255) / 256, 256, 0, s>>>(a);
@@ -781,7 +838,7 @@ int tm_mlp_train(tm_mlp* m, int steps, float lr, float beta1, float beta2, float
         m->loss_cap = steps;
     }
     cudaStream_t s = m->ctx->stream;
-    const int tiles = (m->n + NT - 1) / NT;
+    const int tiles = (m->n + TS - 1) / TS;
     for (int k = 0; k < steps; ++k) {
         const long long st = m->step + 1 + k;
         const float c1 = (float)(1.0 / (1.0 - std::pow((double)beta1, (double)st)));
@@ -816,7 +873,7 @@ int tm_mlp_predict(tm_mlp* m, const float* x, int n, float* y)
     }
     cudaStream_t s = m->ctx->stream;
     MLP_CUDA(cudaMemcpyAsync(m->px, x, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, s));
-    mlp_tile_kernel<false><<<(n + NT - 1) / NT, NT, SM_TOTAL, s>>>(tile_args(m, m->px, n, 0.f, m->py));
+    mlp_tile_kernel<false><<<(n + TS - 1) / TS, NT, SM_TOTAL, s>>>(tile_args(m, m->px, n, 0.f, m->py));
     const int rc = finish(m);
     if (rc != TM_OK) return rc;
     MLP_CUDA(cudaMemcpy(y, m->py, (size_t)n * 2 * sizeof(float), cudaMemcpyDeviceToHost));

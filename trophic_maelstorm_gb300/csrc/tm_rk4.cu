@@ -34,9 +34,9 @@ __device__ __forceinline__ void rk_rhs_cell(const RK4Args<T>& A, const T* S, int
         fP = ((A.cgmax * Wc) * Pc) / wk;
         upt = upt_num / wk;
     } else {
-        // FP32: two reciprocals instead of three divisions
-        const T iwk = T(1) / wk;
-        infil = ((A.alpha * (Pc + A.k2W0)) * (T(1) / (Pc + A.k2))) * Oc;
+        // FP32: two correctly rounded reciprocals instead of three divisions
+        const T iwk = __frcp_rn(wk);
+        infil = ((A.alpha * (Pc + A.k2W0)) * __frcp_rn(Pc + A.k2)) * Oc;
         fP = ((A.cgmax * Wc) * Pc) * iwk;
         upt = upt_num * iwk;
     }
