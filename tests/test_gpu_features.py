@@ -205,3 +205,29 @@ def test_fke_advdiff_matches_oracle(tmg, oracle, L, v):
     want = oracle.fke_advdiff(rho, gam, vx, vy, p.pref, p.gD, p.gV).reshape(L, L)
     np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-14)
     assert got.sum() == pytest.approx(rho[rho >= 1e-10].sum(), rel=1e-12)
+
+
+@pytest.mark.parametrize("model,nf", [("multisp", 1), ("rietkerk", 3)])
+def test_sweep_driver_other_models(tmg, tmp_path, model, nf):
+    """tm_sweep with the MultiSp DP and the Rietkerk models: the sweep table, one
+    prelim file per control value and a final frame of the model's fields."""
+    from trophic_maelstorm_gb300 import io
+    exe = os.path.join(REPO, "trophic_maelstorm_gb300", "lib", "tm_sweep")
+    out = str(tmp_path / model)
+    dt, tmax = ("0.1", "3") if model == "multisp" else ("0.001", "0.05")
+    a1, a2 = ("0.7", "0.8") if model == "multisp" else ("0.9", "1.1")
+    r = subprocess.run([exe, dt, tmax, "24", "3", a1, a2, "2", "0", "M", "--model", model, "--precision", "fp32",
+                        "--seed", "5", "--out", out], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    stats = [f for f in os.listdir(out) if f.startswith("M_P_c_Delta")]
+    assert len(stats) == 1
+    with open(os.path.join(out, stats[0])) as fh:
+        fh.readline()
+        got = np.loadtxt(fh, delimiter=",", ndmin=2)
+    assert got.shape[0] > 0 and np.all(np.isfinite(got))
+    assert set(np.round(got[:, 0], 6)) == {float(a1), float(a2)}
+    assert len(os.listdir(os.path.join(out, "TimeSeries"))) == 2
+    frames = sorted(f for f in os.listdir(out) if f.startswith("FRAME_"))
+    assert len(frames) == 2
+    fr = io.read_frame(os.path.join(out, frames[0]), 24, nf)
+    assert np.all(np.isfinite(fr)) and np.all(fr >= 0)
