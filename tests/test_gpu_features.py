@@ -214,7 +214,7 @@ def test_sweep_driver_other_models(tmg, tmp_path, model, nf):
     from trophic_maelstorm_gb300 import io
     exe = os.path.join(REPO, "trophic_maelstorm_gb300", "lib", "tm_sweep")
     out = str(tmp_path / model)
-    dt, tmax = ("0.1", "3") if model == "multisp" else ("0.001", "0.05")
+    dt, tmax = ("0.1", "3") if model == "multisp" else ("0.002", "1.2")
     a1, a2 = ("0.7", "0.8") if model == "multisp" else ("0.9", "1.1")
     r = subprocess.run([exe, dt, tmax, "24", "3", a1, a2, "2", "0", "M", "--model", model, "--precision", "fp32",
                         "--seed", "5", "--out", out], capture_output=True, text=True)
