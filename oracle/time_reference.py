@@ -1,0 +1,54 @@
+"""Time the reference's own DP integrator against the CPU restatement on one core
+(TEST INFRASTRUCTURE ONLY; needs `make -C oracle ref-perf`, so the reference
+checkout).  Workload: L = 256, one replicate, a = 0.53, b = 2, D = 1, sigma = 1,
+dt = 0.1, 50 steps from rho0 = 1 + U(-0.01, 0.01).
+
+    python oracle/time_reference.py
+"""
+import ctypes as C
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+
+from oracle import oracle as o  # noqa: E402
+
+L, STEPS, A = 256, 50, 0.53
+
+
+def reference_rate(libname):
+    dp = C.POINTER(C.c_double)
+    lib = C.CDLL(os.path.join(HERE, "_ref", libname))
+    lib.ref_percolation_dornic.argtypes = [dp, C.c_int, dp] + [C.c_double] * 7 + [C.c_int, C.c_int, dp, C.c_int]
+    rho0 = 1 + np.random.default_rng(0).uniform(-0.01, 0.01, L * L)
+    tm = np.array([2.0, 3.0, 5.0])
+    rows = np.zeros((1000, 8))
+    t0 = time.perf_counter()
+    lib.ref_percolation_dornic(tm.ctypes.data_as(dp), len(tm), rho0.ctypes.data_as(dp), 5.0, A, 2.0, 1.0, 1.0, 0.1,
+                               1.0, 1, L, rows.ctypes.data_as(dp), 1000)
+    return L * L * STEPS / (time.perf_counter() - t0)
+
+
+def main():
+    o.build()
+    out = {}
+    for name in ("libref_dp_o3.so", "libref_dp.so"):
+        if os.path.exists(os.path.join(HERE, "_ref", name)):
+            out["reference " + name] = reference_rate(name)
+    rho = 1 + np.random.default_rng(0).uniform(-0.01, 0.01, (L, L))
+    t0 = time.perf_counter()
+    o.dp_run(o.dp_params(a=A), rho, 1, STEPS, [STEPS])
+    out["oracle FP64"] = L * L * STEPS / (time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    o.dp_batch_run_f32([o.dp_params(a=A)], [L], [1], [rho.astype(np.float32)], STEPS, 1)
+    out["oracle FP32 batch, 1 thread"] = L * L * STEPS / (time.perf_counter() - t0)
+    for k, v in out.items():
+        print(f"{k:40s} {v:.3g} site-updates/s per core")
+
+
+if __name__ == "__main__":
+    main()
