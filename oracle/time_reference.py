@@ -13,7 +13,8 @@ import time
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-sys.path.insert(0, os.path.dirname(HERE))
+# run as a script, the oracle directory itself is first on the path: put the repository first
+sys.path[:] = [os.path.dirname(HERE)] + [q for q in sys.path if os.path.abspath(q or ".") != HERE]
 
 from oracle import oracle as o  # noqa: E402
 
