@@ -3,7 +3,7 @@
 checkout).  Workload: L = 256, one replicate, a = 0.53, b = 2, D = 1, sigma = 1,
 dt = 0.1, 50 steps from rho0 = 1 + U(-0.01, 0.01).
 
-    python oracle/time_reference.py
+    python oracle/time_reference.py      # median of five interleaved runs per leg
 """
 import ctypes as C
 import os
@@ -34,21 +34,30 @@ def reference_rate(libname):
     return L * L * STEPS / (time.perf_counter() - t0)
 
 
-def main():
-    o.build()
-    out = {}
-    for name in ("libref_dp_o3.so", "libref_dp.so"):
-        if os.path.exists(os.path.join(HERE, "_ref", name)):
-            out["reference " + name] = reference_rate(name)
+def port_rate(fp32):
     rho = 1 + np.random.default_rng(0).uniform(-0.01, 0.01, (L, L))
     t0 = time.perf_counter()
-    o.dp_run(o.dp_params(a=A), rho, 1, STEPS, [STEPS])
-    out["oracle FP64"] = L * L * STEPS / (time.perf_counter() - t0)
-    t0 = time.perf_counter()
-    o.dp_batch_run_f32([o.dp_params(a=A)], [L], [1], [rho.astype(np.float32)], STEPS, 1)
-    out["oracle FP32 batch, 1 thread"] = L * L * STEPS / (time.perf_counter() - t0)
-    for k, v in out.items():
-        print(f"{k:40s} {v:.3g} site-updates/s per core")
+    if fp32:
+        o.dp_batch_run_f32([o.dp_params(a=A)], [L], [1], [rho.astype(np.float32)], STEPS, 1)
+    else:
+        o.dp_run(o.dp_params(a=A), rho, 1, STEPS, [STEPS])
+    return L * L * STEPS / (time.perf_counter() - t0)
+
+
+def main(reps=5):
+    o.build()
+    legs = {}
+    for name in ("libref_dp_o3.so", "libref_dp.so"):
+        if os.path.exists(os.path.join(HERE, "_ref", name)):
+            legs["reference " + name] = lambda n=name: reference_rate(n)
+    legs["oracle FP64"] = lambda: port_rate(False)
+    legs["oracle FP32 batch, 1 thread"] = lambda: port_rate(True)
+    rates = {k: [] for k in legs}
+    for _ in range(reps):              # interleaved, so drifts of a shared machine hit every leg alike
+        for k, f in legs.items():
+            rates[k].append(f())
+    for k, v in rates.items():
+        print(f"{k:40s} median {np.median(v):.3g} site-updates/s per core  (runs: {', '.join('%.3g' % x for x in v)})")
 
 
 if __name__ == "__main__":
