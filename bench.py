@@ -339,6 +339,57 @@ def rietkerk_4096(ctx, tmg, torch, args, steps=10, L=4096, precision=None):
             "kernels_per_step": 2}
 
 
+def config0_plain_fp64(ctx, tmg, torch, steps=200):
+    """Config 0: one 128^2 FP64 DP lattice, a ramped linearly 0.72 -> 0.70 over 1e4 steps, Euler-exact
+    remainder, exact sampler; timed over `steps` steps of the ramp."""
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    L, n_total = 128, 10000
+    inst = tmg.instances([L], [0], 0.72, (0.70 - 0.72) / n_total)
+    b = tmg.Batch(ctx, tmg.dp_model(**MODEL), inst, tmg.TM_FP64)
+    b.upload([init_field(L, np.random.default_rng(0)).astype(np.float64)])
+    b.enqueue_steps(32)
+    ctx.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        b.enqueue_steps(steps)
+        e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    b.close()
+    return {"L": L, "precision": "f64", "ms_per_step": ms, "site_updates_per_s": L * L / (ms * 1e-3),
+            "run_1e4_steps_s": ms * n_total * 1e-3}
+
+
+def config1_rietkerk_batch(ctx, tmg, torch, steps=64):
+    """Config 1: Rietkerk 256^2, R = linspace(0.6, 1.2, 8) x 16 replicates (128 instances), RK4 dt = 1e-3,
+    P ~ U(0,1), W = 0.5, O = 1; per-step time in FP32 and FP64."""
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    L = 256
+    Rs = np.linspace(0.6, 1.2, 8)
+    inst = tmg.instances([L] * 128, list(range(100, 228)), np.repeat(Rs, 16))
+    rng = np.random.default_rng(4)
+    f0 = [np.stack([rng.uniform(0, 1, (L, L)), np.full((L, L), 0.5), np.full((L, L), 1.0)]) for _ in range(128)]
+    out = {}
+    for name, prec in (("f32", tmg.TM_FP32), ("f64", tmg.TM_FP64)):
+        b = tmg.Batch(ctx, tmg.rietkerk_model(), inst, prec)
+        b.upload([f.astype(np.float32 if prec == tmg.TM_FP32 else np.float64) for f in f0])
+        b.enqueue_steps(32)
+        ctx.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            b.enqueue_steps(steps)
+            e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        b.close()
+        sites = 128 * L * L
+        out[name] = {"ms_per_step": ms, "site_updates_per_s": sites / (ms * 1e-3),
+                     "run_1e5_steps_s": ms * 1e5 * 1e-3}
+    return out
+
+
 def fke_advdiff_timing(ctx, L=1024, reps=5):
     """The consumer-movement operator (advdiff_FKE_MultiSp) on one L x L FP64 field:
     the GPU gather (tm_fke_advdiff_device, scratch allocation and synchronisation
@@ -470,6 +521,8 @@ def run_ours(args):
         extras["rietkerk_4096"] = rietkerk_4096(ctx, tmg, torch, args)
         extras["critical_point_search"] = critical_point_search(ctx)
         extras["fke_advdiff"] = fke_advdiff_timing(ctx)
+        extras["config0_dp_128_fp64_ramp"] = config0_plain_fp64(ctx, tmg, torch)
+        extras["config1_rietkerk_256x128"] = config1_rietkerk_batch(ctx, tmg, torch)
 
     hbm, peak_kind = peaks()
     avg_launch_s = statistics.mean(per) * 1e-3

@@ -254,11 +254,12 @@ int tm_batch_power_spectrum(tm_batch* b, int k, int field, double binwidth, doub
  * (rietkerk_bjork_FKE.cpp:195-338, :1735-1749) give for the species.
  *   dev_rho, dev_gamma, dev_vx, dev_vy  device, L*L row-major, `precision`
  *   dev_out  device, L*L; receives the moved field (distinct from the inputs)
- *   gD, gV   host arrays; RD, RV <= 63; 1 <= L <= 46340
- * Computed as a gather (each target sums its sources), so the result has no
- * atomics and does not depend on scheduling; it equals the reference's
- * scatter up to the order of the floating-point additions.  Allocates
- * scratch of 16*L*L bytes and synchronises `stream`. */
+ *   gD, gV   host arrays; RD, RV <= 2^20; 1 <= L <= 46340
+ * Computed as two separable gathers (along rows into per-row-stencil partial
+ * sums, then down columns), so the result has no atomics and does not depend
+ * on scheduling; it equals the reference's scatter up to the order of the
+ * floating-point additions.  Allocates scratch of three L*L arrays of the
+ * precision and two of int, and synchronises `stream`. */
 int tm_fke_advdiff_device(const void* dev_rho, const void* dev_gamma, const void* dev_vx, const void* dev_vy,
                           int precision, int L, double pref, double eps, const double* gD, int RD,
                           const double* gV, int RV, void* dev_out, void* stream);

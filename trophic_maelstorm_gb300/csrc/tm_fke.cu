@@ -1,20 +1,31 @@
-// tm_fke.cu -- FKE advection-diffusion of a consumer field, as a gather.
+// tm_fke.cu -- FKE advection-diffusion of a consumer field, as separable gathers.
 //
 // The reference moves its consumer species with advdiff_FKE_MultiSp
 // (simulations/Rietkerk_FPE/rietkerk_bjork_FKE.cpp:3614-3695) and, on the GPU,
 // with updateMovement (kernel_advdiff_FKE2D.cu:92-180): every source site with
-// rho >= eps scatters its mass through four separable Gaussian kernels
+// rho >= eps scatters its mass through four separable Gaussian stencils
 // (diffusion around the site, advection around the site shifted by
 // round(v * pref), and the two mixed products), the reference kernel with FP64
-// atomicAdd.  Here each target site gathers instead: for every source within
-// reach it multiplies the row and column stencil sums over all periodic images
-// of the target, so there are no atomics and the result does not depend on
-// scheduling.  Reach = max(RD, RV + largest |shift|), the shift bound taken
-// from the velocity field on the device.
+// atomicAdd.  Here the four terms are grouped by their row stencil and
+// gathered in two passes, with no atomics (the result does not depend on
+// scheduling):
+//   pass 1, along rows:  A_D[r][q] = sum over the sources of row r of
+//                                    wDD gD(q - cj) + wDV gV(q - muy)
+//                        A_V[r][q] = the same sum over the sources whose
+//                                    shifted row mux is r, of wDV gD(q - cj) + wVV gV(q - muy)
+//   pass 2, down columns: out[p][q] = sum_r gD(p - r) A_D[r][q] + gV(p - r) A_V[r][q]
+// with wDD = gamma^2 rho, wDV = gamma (1 - gamma) rho, wVV = (1 - gamma)^2 rho,
+// and gD, gV the stencils wrapped onto the periodic lattice (summed over
+// every image, so lattices narrower than a stencil are exact).  A site then
+// costs about (2W + 1)(2 + 2(2S + 1)) + 2RD + 2RV + 2 multiply-adds, W the
+// source window max(RD, RV + S) and S the largest shift, against the
+// (2W + 1)^2 sources a direct gather visits.
 #include "tm_kernels.cuh"
 #include "../../include/tm.h"
 
 #include <cuda_runtime.h>
+
+#include <vector>
 
 namespace {
 
@@ -22,19 +33,6 @@ __device__ __forceinline__ int pmod(int p, int L)
 {
     const int r = p % L;
     return r < 0 ? r + L : r;
-}
-
-// sum of g[|d + k L|] over the images k with |d + k L| <= R
-template <typename T>
-__device__ __forceinline__ T image_sum(const T* g, int R, int d, int L)
-{
-    T s = T(0);
-    int k0 = -((R + d) / L) - 1;
-    for (int k = k0; d + k * L <= R; ++k) {
-        const int e = d + k * L;
-        if (e >= -R) s = s + g[e < 0 ? -e : e];
-    }
-    return s;
 }
 
 template <typename T>
@@ -57,37 +55,66 @@ __global__ void fke_prep_kernel(const T* rho, const T* vx, const T* vy, int L, T
     if ((threadIdx.x & 31) == 0) atomicMax(smax, local);
 }
 
-template <typename T>
-__global__ void fke_gather_kernel(const T* w, const T* gam, const int* mux, const int* muy, const int* smax, int L,
-                                  const T* gD, int RD, const T* gV, int RV, T* out)
+// offsets o of a window [-R, R] taken mod L: each residue once (all of them when 2R+1 >= L)
+__device__ __forceinline__ void window(int R, int L, int& lo, int& hi)
 {
-    __shared__ T sD[64], sV[64];
-    for (int i = threadIdx.x; i <= RD; i += blockDim.x) sD[i] = gD[i];
-    for (int i = threadIdx.x; i <= RV; i += blockDim.x) sV[i] = gV[i];
-    __syncthreads();
+    if (2 * R + 1 >= L) { lo = 0; hi = L - 1; }
+    else { lo = -R; hi = R; }
+}
+
+// pass 1: A_D and A_V of one (row r, column q)
+template <typename T>
+__global__ void fke_rows_kernel(const T* w, const T* gam, const int* mux, const int* muy, const int* smax, int L,
+                                const T* gDw, const T* gVw, int RD, int RV, T* AD, T* AV)
+{
     const int n = L * L;
-    const int W = max(RD, RV + *smax);
-    const bool all = 2 * W + 1 >= L;
-    const int lo = all ? 0 : -W, hi = all ? L - 1 : W;
+    const int S = *smax;
+    int wlo, whi, slo, shi;
+    window(max(RD, RV + S), L, wlo, whi);
+    window(S, L, slo, shi);
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        const int ty = t / L, tx = t - ty * L;
-        T acc = T(0);
-        for (int oy = lo; oy <= hi; ++oy) {
-            const int sy = all ? oy : pmod(ty - oy, L);
-            for (int ox = lo; ox <= hi; ++ox) {
-                const int sx = all ? ox : pmod(tx - ox, L);
-                const int j = sy * L + sx;
-                const T r = w[j];
-                if (r == T(0)) continue;
+        const int r = t / L, q = t - r * L;
+        T ad = T(0), av = T(0);
+        for (int o = wlo; o <= whi; ++o) {
+            const int cj = pmod(q - o, L);
+            const int j = r * L + cj;
+            const T rv = w[j];
+            if (rv == T(0)) continue;
+            const T g = gam[j];
+            const T g2 = g * g;
+            ad = ad + (g2 * rv) * gDw[pmod(q - cj, L)] + ((g - g2) * rv) * gVw[pmod(q - muy[j], L)];
+        }
+        for (int so = slo; so <= shi; ++so) {
+            const int ci = pmod(r - so, L);
+            for (int o = wlo; o <= whi; ++o) {
+                const int cj = pmod(q - o, L);
+                const int j = ci * L + cj;
+                if (mux[j] != r) continue;
+                const T rv = w[j];
+                if (rv == T(0)) continue;
                 const T g = gam[j];
-                const T g2 = g * g;
-                const T SDr = image_sum(sD, RD, ty - sy, L), SDc = image_sum(sD, RD, tx - sx, L);
-                const T SVr = image_sum(sV, RV, ty - mux[j], L), SVc = image_sum(sV, RV, tx - muy[j], L);
-                const T wDV = (g - g2) * r;
-                acc = acc + (g2 * r) * (SDr * SDc) + wDV * (SDr * SVc) + wDV * (SVr * SDc) +
-                      (((T(1) - g) * (T(1) - g)) * r) * (SVr * SVc);
+                av = av + ((g - g * g) * rv) * gDw[pmod(q - cj, L)] +
+                     (((T(1) - g) * (T(1) - g)) * rv) * gVw[pmod(q - muy[j], L)];
             }
         }
+        AD[t] = ad;
+        AV[t] = av;
+    }
+}
+
+// pass 2: out[p][q] = sum_d gD(d) A_D[p - d][q] + gV(d) A_V[p - d][q]
+template <typename T>
+__global__ void fke_cols_kernel(const T* AD, const T* AV, int L, const T* gDw, const T* gVw, int RD, int RV, T* out)
+{
+    const int n = L * L;
+    int dlo, dhi, vlo, vhi;
+    window(RD, L, dlo, dhi);
+    window(RV, L, vlo, vhi);
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int p = t / L, q = t - p * L;
+        T acc = T(0);
+        for (int d = dlo; d <= dhi; ++d) acc = acc + gDw[pmod(d, L)] * AD[pmod(p - d, L) * L + q];
+        for (int d = vlo; d <= vhi; ++d) acc = acc + gVw[pmod(d, L)] * AV[pmod(p - d, L) * L + q];
         out[t] = acc;
     }
 }
@@ -97,27 +124,31 @@ int run(const void* rho, const void* gam, const void* vx, const void* vy, int L,
         const double* gD, int RD, const double* gV, int RV, void* out, cudaStream_t s)
 {
     const size_t n = (size_t)L * L;
-    T *w = nullptr, *dgD = nullptr, *dgV = nullptr;
+    // the stencils wrapped onto the lattice: every image d = delta (mod L) of |d| <= R summed
+    std::vector<double> wd(L, 0.0), wv(L, 0.0);
+    for (int d = -RD; d <= RD; ++d) wd[((d % L) + L) % L] += gD[d < 0 ? -d : d];
+    for (int d = -RV; d <= RV; ++d) wv[((d % L) + L) % L] += gV[d < 0 ? -d : d];
+    std::vector<T> hd(wd.begin(), wd.end()), hv(wv.begin(), wv.end());
+    T *w = nullptr, *AD = nullptr, *AV = nullptr, *dgD = nullptr, *dgV = nullptr;
     int *mx = nullptr, *my = nullptr, *smax = nullptr;
-    T hD[64], hV[64];
-    for (int i = 0; i <= RD; ++i) hD[i] = (T)gD[i];
-    for (int i = 0; i <= RV; ++i) hV[i] = (T)gV[i];
     int rc = TM_OK;
-    if (cudaMalloc(&w, n * sizeof(T)) != cudaSuccess || cudaMalloc(&mx, n * sizeof(int)) != cudaSuccess ||
+    if (cudaMalloc(&w, n * sizeof(T)) != cudaSuccess || cudaMalloc(&AD, n * sizeof(T)) != cudaSuccess ||
+        cudaMalloc(&AV, n * sizeof(T)) != cudaSuccess || cudaMalloc(&mx, n * sizeof(int)) != cudaSuccess ||
         cudaMalloc(&my, n * sizeof(int)) != cudaSuccess || cudaMalloc(&smax, sizeof(int)) != cudaSuccess ||
-        cudaMalloc(&dgD, 64 * sizeof(T)) != cudaSuccess || cudaMalloc(&dgV, 64 * sizeof(T)) != cudaSuccess) {
+        cudaMalloc(&dgD, L * sizeof(T)) != cudaSuccess || cudaMalloc(&dgV, L * sizeof(T)) != cudaSuccess) {
         rc = TM_ERR_NOMEM;
     } else {
         cudaMemsetAsync(smax, 0, sizeof(int), s);
-        cudaMemcpyAsync(dgD, hD, (RD + 1) * sizeof(T), cudaMemcpyHostToDevice, s);
-        cudaMemcpyAsync(dgV, hV, (RV + 1) * sizeof(T), cudaMemcpyHostToDevice, s);
-        const int grid = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+        cudaMemcpyAsync(dgD, hd.data(), L * sizeof(T), cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(dgV, hv.data(), L * sizeof(T), cudaMemcpyHostToDevice, s);
+        const int grid = (int)((n + 255) / 256 < 8192 ? (n + 255) / 256 : 8192);
         fke_prep_kernel<T><<<grid, 256, 0, s>>>((const T*)rho, (const T*)vx, (const T*)vy, L, (T)pref, (T)eps, w, mx, my,
                                                 smax);
-        fke_gather_kernel<T><<<grid, 256, 0, s>>>(w, (const T*)gam, mx, my, smax, L, dgD, RD, dgV, RV, (T*)out);
+        fke_rows_kernel<T><<<grid, 256, 0, s>>>(w, (const T*)gam, mx, my, smax, L, dgD, dgV, RD, RV, AD, AV);
+        fke_cols_kernel<T><<<grid, 256, 0, s>>>(AD, AV, L, dgD, dgV, RD, RV, (T*)out);
         if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) rc = TM_ERR_CUDA;
     }
-    cudaFree(w); cudaFree(mx); cudaFree(my); cudaFree(smax); cudaFree(dgD); cudaFree(dgV);
+    cudaFree(w); cudaFree(AD); cudaFree(AV); cudaFree(mx); cudaFree(my); cudaFree(smax); cudaFree(dgD); cudaFree(dgV);
     (void)cudaGetLastError();
     return rc;
 }
@@ -128,8 +159,8 @@ extern "C" int tm_fke_advdiff_device(const void* dev_rho, const void* dev_gamma,
                                      const void* dev_vy, int precision, int L, double pref, double eps,
                                      const double* gD, int RD, const double* gV, int RV, void* dev_out, void* stream)
 {
-    if (!dev_rho || !dev_gamma || !dev_vx || !dev_vy || !dev_out || !gD || !gV || L < 1 || L > 46340 || RD < 0 || RV < 0 ||
-        RD > 63 || RV > 63)
+    if (!dev_rho || !dev_gamma || !dev_vx || !dev_vy || !dev_out || !gD || !gV || L < 1 || L > 46340 || RD < 0 ||
+        RV < 0 || RD > (1 << 20) || RV > (1 << 20))
         return TM_ERR_INVALID;
     if (precision == TM_FP64)
         return run<double>(dev_rho, dev_gamma, dev_vx, dev_vy, L, pref, eps, gD, RD, gV, RV, dev_out,
