@@ -3,6 +3,7 @@
 // sources by oracle/Makefile.  TEST INFRASTRUCTURE ONLY: used to generate the
 // golden fixtures in tests/golden/.  Declarations restate the definitions'
 // signatures (stochasticSPDP.cpp:940, :549, :1775, :336).
+#include <random>
 #include <vector>
 #include <iostream>
 #include <sstream>
@@ -71,6 +72,24 @@ void ref_rk4_first_order(double* rho, int g, double a, double b, double c, doubl
     vector<double> v(rho, rho + (size_t)g * g);
     RK4_Integrate(v, a, b, c, D, t, dt, dx, g);
     std::memcpy(rho, v.data(), sizeof(double) * g * g);
+}
+
+// n draws from the libstdc++ distributions the reference's Dornic step constructs
+// (stochasticSPDP.cpp:1055-1059): kind 0 std::poisson_distribution<int>(param),
+// kind 1 std::gamma_distribution<double>(param, 1), from std::mt19937_64(seed).
+int ref_libstdcxx_draws(int kind, double param, unsigned long long seed, int n, double* out)
+{
+    std::mt19937_64 rng(seed);
+    for (int i = 0; i < n; ++i) {
+        if (kind == 0) {
+            std::poisson_distribution<int> d(param);
+            out[i] = (double)d(rng);
+        } else {
+            std::gamma_distribution<double> d(param, 1.0);
+            out[i] = d(rng);
+        }
+    }
+    return n;
 }
 
 int ref_logarithm10_time_bins(double t_max, double dt, double* out, int max_n)

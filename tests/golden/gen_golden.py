@@ -20,6 +20,12 @@ ref_dp_ensemble.npz  per-replicate trajectories of percolationDornic_2D
                    reference seeds std::mt19937_64 from std::random_device, so
                    these draws are not reproducible; they are a fixed sample of
                    the reference's ensemble, compared statistically.
+ref_libstdcxx.npz  draws of the libstdc++ poisson_distribution / gamma_distribution
+                   the reference's Dornic step constructs (stochasticSPDP.cpp:1055-1059),
+                   from a seeded std::mt19937_64.
+
+    python tests/golden/gen_golden.py --fke        # only ref_fke.npz
+    python tests/golden/gen_golden.py --libstdcxx  # only ref_libstdcxx.npz
 """
 from __future__ import annotations
 
@@ -58,6 +64,9 @@ def load(names=("dp", "rietkerk", "multisp")):
     d.ref_perc_nodiff.argtypes = [dp, C.c_int, dp] + [C.c_double] * 6 + [C.c_int, dp, C.c_int]
     d.ref_rk4_first_order.argtypes = [dp, C.c_int] + [C.c_double] * 7
     d.ref_logarithm10_time_bins.argtypes = [C.c_double, C.c_double, dp, C.c_int]
+    d.ref_libstdcxx_draws.argtypes = [C.c_int, C.c_double, C.c_ulonglong, C.c_int, dp]
+    if "rietkerk" not in libs:
+        return libs
     r = libs["rietkerk"]
     r.ref_rk_det_steps.argtypes = [dp, C.c_int, C.c_int] + [C.c_double] * 14
     r.ref_rk_stoch_remainder.argtypes = [dp, C.c_int] + [C.c_double] * 12
@@ -187,7 +196,30 @@ def fke(libs, rng):
     return out
 
 
+# means and shapes of the sampler-level comparison with libstdc++
+LIBSTDCXX_POISSON = (0.3, 3.0, 17.0, 50.0, 250.0)
+LIBSTDCXX_GAMMA = (0.4, 1.7, 8.0, 60.0)
+LIBSTDCXX_N = 6000
+
+
+def libstdcxx(libs):
+    """Draws of the libstdc++ Poisson and Gamma distributions the reference's Dornic step
+    constructs per site (stochasticSPDP.cpp:1055-1059), for a sampler-level comparison."""
+    out = {}
+    for kind, params in ((0, LIBSTDCXX_POISSON), (1, LIBSTDCXX_GAMMA)):
+        for k, v in enumerate(params):
+            x = np.zeros(LIBSTDCXX_N)
+            libs["dp"].ref_libstdcxx_draws(kind, v, 1000 + 17 * k + kind, LIBSTDCXX_N, _p(x))
+            out[f"{'poisson' if kind == 0 else 'gamma'}_{k}"] = x.astype(np.float32)
+    out["poisson_params"] = np.array(LIBSTDCXX_POISSON)
+    out["gamma_params"] = np.array(LIBSTDCXX_GAMMA)
+    return out
+
+
 def main():
+    if "--libstdcxx" in sys.argv:
+        np.savez_compressed(os.path.join(HERE, "ref_libstdcxx.npz"), **libstdcxx(load(("dp",))))
+        return
     if "--fke" in sys.argv:
         np.savez_compressed(os.path.join(HERE, "ref_fke.npz"), **fke(load(("fke",)), np.random.default_rng(11)))
         return
@@ -204,6 +236,7 @@ def main():
         for k, v in e.items():
             ens[f"{tag}_{k}"] = v
     np.savez_compressed(os.path.join(HERE, "ref_dp_ensemble.npz"), **ens)
+    np.savez_compressed(os.path.join(HERE, "ref_libstdcxx.npz"), **libstdcxx(libs))
     print("wrote", os.listdir(HERE))
 
 

@@ -94,3 +94,37 @@ def test_dornic_draw_law(oracle, dtype, m, mu1):
     x, st = oracle.sample("dornic", 60000, seed=17, m=m, mu1=mu1, inv_lambda=1.0, dtype=dtype)
     assert st == 0
     assert stats.kstest(2.0 * x.astype(np.float64), stats.ncx2(2 * mu1, 2 * m).cdf).pvalue > 1e-3
+
+
+def _libstdcxx():
+    import os
+    return np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_libstdcxx.npz"))
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_poisson_matches_libstdcxx(oracle, dtype):
+    """The oracle's Poisson draws against the libstdc++ poisson_distribution the reference
+    constructs per site: chi-square homogeneity of the binned counts, p > 1e-3, at every mean."""
+    z = _libstdcxx()
+    for k, m in enumerate(z["poisson_params"]):
+        ref = z[f"poisson_{k}"].astype(np.int64)
+        x, st = oracle.sample("poisson", len(ref), seed=31 + k, m=float(m), dtype=dtype)
+        assert st == 0
+        x = x.astype(np.int64)
+        lo, hi = np.percentile(np.concatenate([ref, x]), [0.5, 99.5]).astype(int)
+        edges = np.unique(np.linspace(lo, hi + 1, min(30, hi - lo + 2)).astype(int))
+        a = np.histogram(np.clip(x, lo, hi), edges)[0]
+        b = np.histogram(np.clip(ref, lo, hi), edges)[0]
+        keep = (a + b) > 0
+        assert stats.chi2_contingency(np.stack([a[keep], b[keep]]))[1] > 1e-3, m
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_gamma_matches_libstdcxx(oracle, dtype):
+    """The oracle's Gamma draws against the libstdc++ gamma_distribution: two-sample KS, p > 1e-3."""
+    z = _libstdcxx()
+    for k, shape in enumerate(z["gamma_params"]):
+        ref = z[f"gamma_{k}"].astype(np.float64)
+        x, st = oracle.sample("gamma", len(ref), seed=57 + k, k=float(shape), dtype=dtype)
+        assert st == 0
+        assert stats.ks_2samp(x.astype(np.float64), ref).pvalue > 1e-3, shape
