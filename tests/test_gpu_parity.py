@@ -301,3 +301,17 @@ def test_fp32_state_is_statistically_equivalent_to_fp64(tmg, ctx):
     assert r["status"] == [0, 0]
     assert r["max_abs_z_rho"] < 3.5 and r["max_abs_z_surv"] < 3.5
     assert r["min_ks_p"] > 0.01 / n_t
+
+
+def test_sweep_rows_do_not_depend_on_the_split(tmg, ctx):
+    """The sharded sweep's blocks (what each rank of critical_exp_delta(distributed=True)
+    runs) reproduce the single-batch rows bit for bit: keys depend on the value, not the rank."""
+    from trophic_maelstorm_gb300 import api
+    args = (np.ones(16 * 16), 10.0, 2.0, 1.0, 1.0, 0.1, 1.0, 3, 16, 7, tmg.TM_FP32)
+    avals = api.linspace(0.5, 0.6, 5)
+    full = api._sweep_block(ctx, list(range(5)), avals, *args)
+    parts = {}
+    for rank in range(3):
+        parts.update(api._sweep_block(ctx, api.shard_indices(5, rank, 3), avals, *args))
+    for ia in range(5):
+        assert np.array_equal(full[ia][0], parts[ia][0]) and np.array_equal(full[ia][1], parts[ia][1])

@@ -421,25 +421,75 @@ def percolation_dornic_2d(t_meas, Rh0, t_max, a, b, D, sigma, dt, dx, r, g, *, s
     return replicate_rows(a, g, times, n_early, mean, act), st
 
 
-def critical_exp_delta(Rho_0, div, t_max, a_start, a_end, b, D, sigma, dt, dx, r, g, *, seed=0,
-                       precision=T.TM_FP64, ctx: Context | None = None):
-    """The a-sweep of stochasticSPDP.cpp:1309-1422 in one batch: div values of a
-    (linspace), r replicates each, rows concatenated in a order."""
-    ctx = ctx or Context(0)
+def shard_indices(n, rank, world):
+    """The contiguous block of range(n) that one of `world` ranks takes (the first
+    n % world ranks take one more): the static split of a sweep's control values."""
+    base, extra = divmod(int(n), int(world))
+    start = rank * base + min(rank, extra)
+    return list(range(start, start + base + (1 if rank < extra else 0)))
+
+
+def _sweep_block(ctx, indices, avals, Rho_0, t_max, b, D, sigma, dt, dx, r, g, seed, precision):
+    """Rows and status of the control values `indices` of a sweep, in one batch:
+    {index: (rows, status of its r replicates)}.  Replicate j of value i has the
+    Philox key seed + i r + j whichever rank runs it."""
+    if not indices:
+        return {}
     t_meas = logarithm10_time_bins(t_max, dt)
     steps, times, n_early = reference_step_grid(t_meas, dt)
-    avals = linspace(a_start, a_end, div)
     Ls, seeds, av = [], [], []
-    for ia, a in enumerate(avals):
+    for ia in indices:
         for j in range(r):
-            Ls.append(g); seeds.append(seed + ia * r + j); av.append(a)
+            Ls.append(g); seeds.append(seed + ia * r + j); av.append(avals[ia])
     inst = instances(Ls, seeds, av)
     model = dp_model(b=b, D=D, sigma=sigma, dt=dt, dx=dx)
     dtype = np.float64 if precision == T.TM_FP64 else np.float32
     init = pack([np.asarray(Rho_0, np.float64).reshape(g, g)] * len(Ls), inst, 1, dtype)
     obs, st, _ = run_dp(ctx, model, inst, init, max(steps), steps, precision)
-    rows = []
-    for ia, a in enumerate(avals):
-        sl = slice(ia * r, (ia + 1) * r)
-        rows.append(replicate_rows(a, g, times, n_early, obs[:, sl, 0].T, obs[:, sl, 1].T))
-    return np.concatenate(rows), st
+    out = {}
+    for k, ia in enumerate(indices):
+        sl = slice(k * r, (k + 1) * r)
+        out[ia] = (replicate_rows(avals[ia], g, times, n_early, obs[:, sl, 0].T, obs[:, sl, 1].T), st[sl])
+    return out
+
+
+def gather_blocks(blocks, rank, world):
+    """Every rank's {index: ...} blocks merged on rank 0 (a host gather over the
+    initialised torch.distributed group); None on the other ranks."""
+    if world == 1:
+        return dict(blocks)
+    import torch.distributed as dist
+    got = [None] * world if rank == 0 else None
+    dist.gather_object(blocks, got, dst=0)
+    if rank != 0:
+        return None
+    merged = {}
+    for part in got:
+        merged.update(part)
+    return merged
+
+
+def critical_exp_delta(Rho_0, div, t_max, a_start, a_end, b, D, sigma, dt, dx, r, g, *, seed=0,
+                       precision=T.TM_FP64, ctx: Context | None = None, distributed=False):
+    """The a-sweep of stochasticSPDP.cpp:1309-1422 in one batch: div values of a
+    (linspace), r replicates each, rows concatenated in a order.
+
+    distributed=True splits the a-values over the ranks of the initialised
+    torch.distributed group (one GPU each): every rank runs its contiguous block
+    as one batch, and rank 0 gathers the rows on the host and returns the same
+    rows as a single-GPU run (the replicates' keys do not depend on the split);
+    the other ranks return (None, None)."""
+    ctx = ctx or Context(0)
+    avals = linspace(a_start, a_end, div)
+    if distributed:
+        import torch.distributed as dist
+        rank, world = dist.get_rank(), dist.get_world_size()
+    else:
+        rank, world = 0, 1
+    mine = shard_indices(div, rank, world)
+    blocks = _sweep_block(ctx, mine, avals, Rho_0, t_max, b, D, sigma, dt, dx, r, g, seed, precision)
+    merged = gather_blocks(blocks, rank, world)
+    if merged is None:
+        return None, None
+    return (np.concatenate([merged[ia][0] for ia in range(div)]),
+            np.concatenate([merged[ia][1] for ia in range(div)]))
