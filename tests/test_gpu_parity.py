@@ -315,3 +315,44 @@ def test_sweep_rows_do_not_depend_on_the_split(tmg, ctx):
         parts.update(api._sweep_block(ctx, api.shard_indices(5, rank, 3), avals, *args))
     for ia in range(5):
         assert np.array_equal(full[ia][0], parts[ia][0]) and np.array_equal(full[ia][1], parts[ia][1])
+
+
+def test_full_sweep_batch_matches_oracle_on_sampled_instances(tmg, oracle, ctx):
+    """The bench's whole workload -- L in {64..1024} x 32 replicates x 16 a (2560 instances,
+    715,128,832 sites, FP32) -- advanced two steps in one batch: sampled instances of every L
+    equal the oracle bit for bit, and every instance keeps a finite, non-negative state."""
+    torch = pytest.importorskip("torch")
+    LS, REPS, NA = (64, 128, 256, 512, 1024), 32, 16
+    avals = np.geomspace(0.53 * 0.98, 0.53 * 1.02, NA)
+    Ls, seeds, av = [], [], []
+    for L in LS:
+        for a in avals:
+            for r in range(REPS):
+                Ls.append(L); seeds.append(1_000_003 * len(Ls) + 17); av.append(float(a))
+    inst = tmg.instances(Ls, seeds, av)
+    b = tmg.Batch(ctx, tmg.dp_model(), inst, tmg.TM_FP32)
+    total, off, _ = tmg.layout(inst, 1)
+    buf = torch.zeros(total, dtype=torch.float32, device="cuda")
+    for k, L in enumerate(Ls):
+        buf[int(off[k]):int(off[k]) + L * L] = 1.0
+    rng = np.random.default_rng(123)
+    picks = [k for i, L in enumerate(LS) for k in (i * NA * REPS + int(rng.integers(NA * REPS)),)]
+    picks.append(len(Ls) - 1)
+    init = {}
+    for k in picks:
+        L = Ls[k]
+        init[k] = (1.0 + rng.uniform(-0.01, 0.01, (L, L))).astype(np.float32)
+        buf[int(off[k]):int(off[k]) + L * L] = torch.from_numpy(init[k].reshape(-1)).cuda()
+    torch.cuda.synchronize()
+    b.upload_device(buf.data_ptr())
+    ctx.sync()
+    del buf
+    obs, st = b.advance(2, [2])
+    assert int(np.bitwise_or.reduce(st)) == 0
+    m = obs[0, :, 0]
+    assert np.all(np.isfinite(m)) and np.all(m > 0)
+    for k in picks:
+        p = oracle.dp_params(a=av[k])
+        _, _, want, _ = oracle.dp_run(p, init[k], seeds[k], 2, [2])
+        assert np.array_equal(b.snapshot(k), want), (k, Ls[k])
+    b.close()
