@@ -169,7 +169,7 @@ def test_rietkerk_matches_oracle(tmg, oracle, ctx, precision, sampler):
 
 def test_rietkerk_noise_off_matches_reference(tmg, ctx, golden):
     """Noise-off Rietkerk RK4 (f_2D / RK4_Integrate) on the GPU against the reference's
-    own output, to 1e-10 relative (the spec noise-off bar)."""
+    own output, to 1e-10 relative (the noise-off parity bar)."""
     g = golden["pins"]
     for tag in ("rkdet_a", "rkdet_b"):
         L, n, dt, R = g[f"{tag}_meta"]
