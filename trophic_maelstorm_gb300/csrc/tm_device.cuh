@@ -527,7 +527,7 @@ __device__ __forceinline__ T dornic_draw(Stream<T>& g, T m, T mu1, T inv_lambda,
 // dornic_draw does, so when it returns without deferring the value equals
 // dornic_draw's bit for bit; otherwise (*deferred) the caller recomputes the
 // site with dornic_draw.
-constexpr int kFastInv = 24;
+constexpr int kFastInv = 32;
 static_assert(kFastInv % 4 == 0, "the inversion takes four terms per trip");
 
 __device__ __forceinline__ float dornic_draw_fast(uint64_t seed, uint32_t site, int64_t step, float m, float mu1,
