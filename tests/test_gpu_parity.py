@@ -356,3 +356,36 @@ def test_full_sweep_batch_matches_oracle_on_sampled_instances(tmg, oracle, ctx):
         _, _, want, _ = oracle.dp_run(p, init[k], seeds[k], 2, [2])
         assert np.array_equal(b.snapshot(k), want), (k, Ls[k])
     b.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32"])
+@pytest.mark.parametrize("R", [4, 8, 16])
+def test_large_absorbing_regions_match_oracle(tmg, oracle, ctx, precision, R):
+    """Lattices that are mostly absorbing (L = 20 < 32, ragged L = 70 and 128, one small
+    occupied patch, subcritical a so the empty area grows), 80 steps for every task height:
+    the fields equal the oracle bit for bit, also after an upload in the middle and across
+    graph chunks."""
+    dtype = np.float64 if precision == 0 else np.float32
+    Ls = [20, 70, 128]
+    rng = np.random.default_rng(R)
+    init = []
+    for L in Ls:
+        f = np.zeros((L, L))
+        f[L // 3: L // 3 + max(2, L // 6), L // 4: L // 4 + max(2, L // 5)] = rng.uniform(0.5, 1.5)
+        init.append(f.astype(dtype))
+    seeds = [31, 32, 33]
+    inst = tmg.instances(Ls, seeds, 0.35)
+    b = tmg.Batch(ctx, tmg.dp_model(), inst, precision)
+    b.set_launch(R, 2)
+    b.upload(init)
+    b.advance(45)
+    mid = b.download()
+    b.upload(mid, step=45)
+    b.advance(35)
+    fin = b.download()
+    for k, L in enumerate(Ls):
+        p = oracle.dp_params(a=0.35)
+        _, _, want, _ = oracle.dp_run(p, init[k], seeds[k], 80, [80])
+        assert np.array_equal(fin[k], want), L
+        assert np.count_nonzero(want) < 0.5 * L * L      # the skipped region exists
+    b.close()
