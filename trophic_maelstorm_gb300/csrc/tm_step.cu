@@ -42,7 +42,10 @@ __host__ __device__ __forceinline__ size_t warp_scratch_bytes(int rows_cap)
     return (size_t)rows_cap * 32 * (3 * sizeof(T) + 2 * sizeof(unsigned short));
 }
 
-template <typename T, int REM>
+// SAMP is the sampler (0 exact, 1 Gaussian above 100, 2 noise off) as a
+// compile-time constant: each instantiation carries only its own sampler's
+// code, which keeps the loop body small for the instruction cache.
+template <typename T, int REM, int SAMP>
 __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_kernel(const DornicArgs<T> A)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -92,8 +95,8 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
             if (lane == w - 1) east = src[(long long)y * L + xe];
             const T nsum = ((north + south) + west) + east;
             const T alpha = A.dcoef * nsum;
-            const bool live = act && !(alpha == T(0) && cur == T(0)) && A.sampler != 2;
-            if (!live) Wres[r * 32 + lane] = (A.sampler == 2 && act) ? a1 * cur + a2 * alpha : T(0);
+            const bool live = act && !(alpha == T(0) && cur == T(0)) && SAMP != 2;
+            if (!live) Wres[r * 32 + lane] = (SAMP == 2 && act) ? a1 * cur + a2 * alpha : T(0);
             const unsigned bal = __ballot_sync(0xffffffffu, live);
             if (live) {
                 const int pos = nq + __popc(bal & lt_mask);
@@ -121,7 +124,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
                     const int li = Wqi[j];
                     const int site = (y0 + (li >> 5)) * L + x0 + (li & 31);
                     const float v = dornic_draw_fast(seed, (uint32_t)site, step, Wqm[j], Wqmu[j], inv_lambda,
-                                                     A.sampler, tab, deferred);
+                                                     SAMP, tab, deferred);
                     if (!deferred) Wres[li] = v;
                 }
                 const unsigned bal = __ballot_sync(0xffffffffu, has && deferred);
@@ -140,7 +143,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
             const int site = (y0 + (li >> 5)) * L + x0 + (li & 31);
             Stream<T> g;
             g.init(seed, (uint32_t)site, step);
-            Wres[li] = dornic_draw(g, Wqm[j], Wqmu[j], inv_lambda, A.sampler, tab);
+            Wres[li] = dornic_draw(g, Wqm[j], Wqmu[j], inv_lambda, SAMP, tab);
             st |= g.status;
         }
         __syncwarp();
@@ -174,26 +177,40 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
     }
 }
 
+template <typename T, int REM, int SAMP>
+cudaError_t launch_dornic_t(const DornicArgs<T>& a, int grid, int block, size_t smem, cudaStream_t s)
+{
+    static bool attr_set = false;
+    if (!attr_set) {
+        const int full = (int)(warp_scratch_bytes<T>(kMaxRowsPerTask) * kWarps);
+        const cudaError_t e =
+            cudaFuncSetAttribute(dornic_step_kernel<T, REM, SAMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, full);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    dornic_step_kernel<T, REM, SAMP><<<grid, block, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <typename T, int REM>
+cudaError_t launch_dornic_r(const DornicArgs<T>& a, int grid, int block, size_t smem, cudaStream_t s)
+{
+    if (a.sampler == 0) return launch_dornic_t<T, REM, 0>(a, grid, block, smem, s);
+    if (a.sampler == 1) return launch_dornic_t<T, REM, 1>(a, grid, block, smem, s);
+    if (a.sampler == 2) return launch_dornic_t<T, REM, 2>(a, grid, block, smem, s);
+    return cudaErrorInvalidValue;
+}
+
 template <typename T>
 cudaError_t launch_dornic(const DornicArgs<T>& a, int rem, int grid, int block, cudaStream_t s)
 {
     if (a.n_tasks <= 0) return cudaSuccess;
     if (block != 32 * kWarps || a.rows_cap < 1 || a.rows_cap > kMaxRowsPerTask) return cudaErrorInvalidValue;
     const size_t smem = warp_scratch_bytes<T>(a.rows_cap) * kWarps;
-    static bool attr_set[3] = {false, false, false};
-    const int full = (int)(warp_scratch_bytes<T>(kMaxRowsPerTask) * kWarps);
-    cudaError_t e = cudaSuccess;
-    if (!attr_set[rem]) {
-        if (rem == 0) e = cudaFuncSetAttribute(dornic_step_kernel<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, full);
-        else if (rem == 1) e = cudaFuncSetAttribute(dornic_step_kernel<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, full);
-        else e = cudaFuncSetAttribute(dornic_step_kernel<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, full);
-        if (e != cudaSuccess) return e;
-        attr_set[rem] = true;
-    }
-    if (rem == 0) dornic_step_kernel<T, 0><<<grid, block, smem, s>>>(a);
-    else if (rem == 1) dornic_step_kernel<T, 1><<<grid, block, smem, s>>>(a);
-    else dornic_step_kernel<T, 2><<<grid, block, smem, s>>>(a);
-    return cudaGetLastError();
+    if (rem == 0) return launch_dornic_r<T, 0>(a, grid, block, smem, s);
+    if (rem == 1) return launch_dornic_r<T, 1>(a, grid, block, smem, s);
+    if (rem == 2) return launch_dornic_r<T, 2>(a, grid, block, smem, s);
+    return cudaErrorInvalidValue;
 }
 template cudaError_t launch_dornic<float>(const DornicArgs<float>&, int, int, int, cudaStream_t);
 template cudaError_t launch_dornic<double>(const DornicArgs<double>&, int, int, int, cudaStream_t);
