@@ -77,10 +77,19 @@ __global__ void __launch_bounds__(RK_THREADS, 3) rk4_tile_kernel(const RK4Args<T
         const T* __restrict__ W0 = A.in + off + fs;
         const T* __restrict__ O0 = A.in + off + 2 * fs;
         __syncthreads();  // previous tile done with shared memory
+        // halo coordinates lie within RK_H of [0, L + tile), so one wrap is enough
+        // once L covers the tile and its halo; smaller lattices take the modulo
+        const bool one_wrap = L >= RK_RY && L >= RK_RX;
         for (int c = tid; c < RK_RN; c += RK_THREADS) {
             const int ry = c / RK_RX, rx = c - ry * RK_RX;
-            int gy = (y0 - RK_H + ry) % L; if (gy < 0) gy += L;
-            int gx = (x0 - RK_H + rx) % L; if (gx < 0) gx += L;
+            int gy = y0 - RK_H + ry, gx = x0 - RK_H + rx;
+            if (one_wrap) {
+                gy = gy < 0 ? gy + L : (gy >= L ? gy - L : gy);
+                gx = gx < 0 ? gx + L : (gx >= L ? gx - L : gx);
+            } else {
+                gy %= L; if (gy < 0) gy += L;
+                gx %= L; if (gx < 0) gx += L;
+            }
             const long long gi = (long long)gy * L + gx;
             X0[c] = P0[gi];
             X0[RK_RN + c] = W0[gi];
