@@ -389,3 +389,28 @@ def test_large_absorbing_regions_match_oracle(tmg, oracle, ctx, precision, R):
         assert np.array_equal(fin[k], want), L
         assert np.count_nonzero(want) < 0.5 * L * L      # the skipped region exists
     b.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32"])
+def test_rietkerk_bulk_copied_tiles_match_oracle(tmg, oracle, ctx, precision):
+    """Lattices where the RK4 tiles take the bulk-copy path (L % 4 == 0, tiles not wrapping
+    in x: L = 200 and 256) beside ones that take per-thread loads (L = 130, L = 132): fields
+    equal the oracle bit for bit."""
+    model = tmg.rietkerk_model()
+    Ls = [200, 256, 130, 132]
+    R = [0.7, 0.9, 1.1, 1.0]
+    dtype = np.float64 if precision == 0 else np.float32
+    rng = np.random.default_rng(8)
+    init = [np.stack([rng.uniform(0, 1, (L, L)), 0.5 + rng.uniform(-0.1, 0.1, (L, L)),
+                      1.0 + rng.uniform(-0.1, 0.1, (L, L))]).astype(dtype) for L in Ls]
+    seeds = [41, 42, 43, 44]
+    inst = tmg.instances(Ls, seeds, R)
+    b = tmg.Batch(ctx, model, inst, precision)
+    b.upload(init)
+    b.advance(6)
+    fin = b.download()
+    for k, L in enumerate(Ls):
+        p = oracle.rk_params(R=R[k])
+        _, _, want, _ = oracle.rk_run(p, init[k], seeds[k], 6, [6])
+        assert np.array_equal(fin[k], want), L
+    b.close()

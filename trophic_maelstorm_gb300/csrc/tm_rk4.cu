@@ -55,16 +55,47 @@ __device__ __forceinline__ void rk_rhs_cell(const RK4Args<T>& A, const T* S, int
 // interior cell depends on -- so the interior is exact after stage 3.  Stage
 // inputs ping-pong between two shared buffers, so each stage needs one barrier
 // and no value is held in registers across it.
+// Tile rows by bulk copy: for a tile that does not wrap in x on a lattice with
+// L % 4 == 0, each of the 3 x RK_RY halo rows is a contiguous RK_RX-float segment
+// starting on a 16-byte boundary (instance offsets and field strides are
+// multiples of 32 elements), so one thread issues them as cp.async.bulk copies
+// completing on an mbarrier instead of 256 threads loading 5184 values.
+constexpr int kRkWaitLimit = 1 << 22;   // polls of the tile's copies before the CTA gives up
+
+__device__ __forceinline__ uint32_t rk_saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ bool rk_bar_wait(uint32_t bar, uint32_t parity)
+{
+    for (int i = 0; i < kRkWaitLimit; ++i) {
+        uint32_t ok;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}\n"
+                     : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+        if (ok) return true;
+        if (i > 16) __nanosleep(32);
+    }
+    return false;
+}
+
 template <typename T, bool DET>
 __global__ void __launch_bounds__(RK_THREADS, 3) rk4_tile_kernel(const RK4Args<T> A)
 {
     extern __shared__ __align__(16) unsigned char rk_smem[];
+    __shared__ __align__(8) uint64_t tile_bar;
+    __shared__ int tile_bulk;
     T* const X0 = reinterpret_cast<T*>(rk_smem);          // [3][RK_RN] stage-0 input
     T* const MA = X0 + 3 * RK_RN;                           // [3][RK_RN] stage inputs (ping)
     T* const MB = MA + 3 * RK_RN;                           // [3][RK_RN] (pong)
     T* const ACC = MB + 3 * RK_RN;                          // [3][RK_TX*RK_TY] weighted sum of K
     constexpr int NI = RK_TX * RK_TY;
     const int tid = threadIdx.x;
+    const uint32_t bar = rk_saddr(&tile_bar);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    uint32_t phase = 0;
     for (int t = blockIdx.x; t < A.n_tasks; t += gridDim.x) {
         const int4 tk = A.tasks[t];
         const int k = tk.x;
@@ -80,6 +111,48 @@ __global__ void __launch_bounds__(RK_THREADS, 3) rk4_tile_kernel(const RK4Args<T
         // halo coordinates lie within RK_H of [0, L + tile), so one wrap is enough
         // once L covers the tile and its halo; smaller lattices take the modulo
         const bool one_wrap = L >= RK_RY && L >= RK_RX;
+        {
+            // one halo row per thread (3 x RK_RY rows): the block takes the bulk path
+            // only if every row start is 16-byte aligned
+            constexpr int kRows = 3 * RK_RY;
+            const bool shape = sizeof(T) == 4 && one_wrap && (L & 3) == 0 && x0 >= RK_H && x0 + RK_TX + RK_H <= L;
+            const T* src = nullptr;
+            bool aligned = true;
+            if (shape && tid < kRows) {
+                const int f = tid / RK_RY, ry = tid - f * RK_RY;
+                int gy = y0 - RK_H + ry;
+                gy = gy < 0 ? gy + L : (gy >= L ? gy - L : gy);
+                src = (f == 0 ? P0 : (f == 1 ? W0 : O0)) + (long long)gy * L + (x0 - RK_H);
+                aligned = ((uintptr_t)src & 15u) == 0;
+            }
+            const bool bulk = shape && __syncthreads_and(aligned);
+            if (bulk) {
+                constexpr uint32_t row_bytes = RK_RX * sizeof(T);
+                static_assert((RK_RX * sizeof(float)) % 16 == 0 && (RK_RN * sizeof(float)) % 16 == 0, "bulk rows");
+                if (tid == 0)
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                                 :: "r"(bar), "r"((uint32_t)kRows * row_bytes) : "memory");
+                __syncthreads();
+                if (tid < kRows) {
+                    const int f = tid / RK_RY, ry = tid - f * RK_RY;
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+                                 "[%0], [%1], %2, [%3];"
+                                 :: "r"(rk_saddr(X0 + f * RK_RN + ry * RK_RX)), "l"(src), "r"(row_bytes), "r"(bar)
+                                 : "memory");
+                }
+            }
+            if (tid == 0) tile_bulk = bulk ? 1 : 0;
+        }
+        __syncthreads();
+        if (tile_bulk) {
+            const bool ok = rk_bar_wait(bar, phase);
+            phase ^= 1u;
+            if (__syncthreads_or(!ok)) {          // copies did not complete: report and stop
+                if (tid == 0) atomicOr(A.it.status + k, TM_STATUS_CAP_BIT);
+                return;
+            }
+        } else
         for (int c = tid; c < RK_RN; c += RK_THREADS) {
             const int ry = c / RK_RX, rx = c - ry * RK_RX;
             int gy = y0 - RK_H + ry, gx = x0 - RK_H + rx;
