@@ -543,7 +543,7 @@ def run_ours(args):
                            parallelism=f"replicas x{world}"),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": "dornic_step_kernel<float, euler>", "alg_bytes_per_site": BYTES_PER_SITE_FP32,
+                         "kernel": "dornic_step_kernel<float, euler, exact sampler>", "alg_bytes_per_site": BYTES_PER_SITE_FP32,
                          "avg_launch_ms": avg_launch_s * 1e3},
             "cpu_baseline": cpu,
             "e2e": None if e2e is None else {"value": e2e, "unit": "site-updates/s",
