@@ -33,13 +33,54 @@ __device__ __forceinline__ T rem_f(T x, T b, T c, int cubic)
 }
 
 // Per-warp shared scratch for one task of up to rows_cap rows: the Dornic draw
-// of every site (res), and the queue of live sites (index, Poisson mean, shape).
+// of every site (res), the queue of live sites (Poisson mean, shape, index),
+// the list of sites left to the general sampler, and up to 31 of those carried
+// over from earlier tasks (instance, site, Poisson mean, shape).
 constexpr int kWarps = 8;
 
 template <typename T>
 __host__ __device__ __forceinline__ size_t warp_scratch_bytes(int rows_cap)
 {
-    return (size_t)rows_cap * 32 * (3 * sizeof(T) + 2 * sizeof(unsigned short));
+    return (size_t)rows_cap * 32 * (3 * sizeof(T) + 2 * sizeof(unsigned short)) + 32 * (2 * sizeof(T) + 8);
+}
+
+// Remainder, clamp and status bits of one site after its Dornic draw.
+template <typename T, int REM>
+__device__ __forceinline__ T finish_site(const DornicArgs<T>& A, T rs, T bi, unsigned& st)
+{
+    T res;
+    if (REM == 0) {
+        res = rs / (T(1) + (bi * rs) * A.dt);
+    } else if (REM == 1) {
+        const T k1 = rem_f(rs, bi, A.c, A.cubic);
+        const T k2 = rem_f(rs + A.dt2 * k1, bi, A.c, A.cubic);
+        const T k3 = rem_f(rs + A.dt2 * k2, bi, A.c, A.cubic);
+        const T k4 = rem_f(rs + A.dt * k3, bi, A.c, A.cubic);
+        res = rs + A.dt6 * (((k1 + T(2) * k2) + T(2) * k3) + k4);
+    } else {
+        res = rs;
+    }
+    if (REM != 2) {
+        if (res < A.ceps && res >= A.clo) res = T(0);
+        st |= value_status(res);
+    }
+    return res;
+}
+
+// One site through the general sampler, then finished and stored.  The draw
+// depends only on (seed, site, step), so it may run in any later pass of the
+// same warp.
+template <typename T, int REM, int SAMP>
+__device__ __forceinline__ void draw_general_site(const DornicArgs<T>& A, const SmemTab<T>& tab, long long step,
+                                                  int k, uint32_t site, T m, T mu1)
+{
+    Stream<T> g;
+    g.init(A.it.seed[k], site, step);
+    const T rs = dornic_draw(g, m, mu1, (T)A.it.consts[k].y, SAMP, tab);
+    const long long o = A.it.off[k] + (long long)site;
+    unsigned st = g.status;
+    A.out[o] = finish_site<T, REM>(A, rs, A.site_b ? A.site_b[o] : A.b, st);
+    if (st) atomicOr(A.it.status + k, st);
 }
 
 // SAMP is the sampler (0 exact, 1 Gaussian above 100, 2 noise off) as a
@@ -50,6 +91,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ SmemTab<T> tab;
+    __shared__ unsigned defer_rows[kWarps][32];
     tab.fill();
     __syncthreads();
     const int cap = A.rows_cap * 32;
@@ -57,123 +99,154 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
     T* const Wres = reinterpret_cast<T*>(wbase);
     T* const Wqm = Wres + cap;
     T* const Wqmu = Wqm + cap;
-    unsigned short* const Wqi = reinterpret_cast<unsigned short*>(Wqmu + cap);
+    T* const Cm = Wqmu + cap;
+    T* const Cmu = Cm + 32;
+    int* const Ck = reinterpret_cast<int*>(Cmu + 32);
+    uint32_t* const Cs = reinterpret_cast<uint32_t*>(Ck + 32);
+    unsigned short* const Wqi = reinterpret_cast<unsigned short*>(Cs + 32);
     unsigned short* const Wdef = Wqi + cap;
+    unsigned* const Wrows = defer_rows[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
     const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int nw = (int)((gridDim.x * blockDim.x) >> 5);
     const long long step = (A.step_base ? *A.step_base : 0LL) + A.step_off;
-    for (int t = gw; t < A.n_tasks; t += nw) {
-        const int4 tk = A.tasks[t];
-        const int k = tk.x;
-        if (A.it.alive != nullptr && A.it.alive[k] == 0) continue;
-        const int L = A.it.L[k];
-        const T* __restrict__ src = A.in + A.it.off[k];
-        T* __restrict__ dst = A.out + A.it.off[k];
-        const Dc4 cs = A.it.consts[k];
-        const T pm = (T)cs.x, inv_lambda = (T)cs.y, a1 = (T)cs.z, a2 = (T)cs.w;
-        const int x0 = tk.y, y0 = tk.z, rows = tk.w;
-        const int w = min(32, L - x0);
-        const int x = x0 + lane;
-        const bool act = lane < w;
-        const int xw = (x0 == 0) ? L - 1 : x0 - 1;
-        const int xe = (x0 + w == L) ? 0 : x0 + w;
-        const int yn = (y0 == 0) ? L - 1 : y0 - 1;
-        // pass 1: stream the rows, form alpha_i, resolve absorbing sites and the
-        // noise-off mean directly, queue the live sites (row-major order)
-        T north = act ? src[(long long)yn * L + x] : T(0);
-        T cur = act ? src[(long long)y0 * L + x] : T(0);
-        int nq = 0;
-        for (int r = 0; r < rows; ++r) {
-            const int y = y0 + r;
-            const int ys = (y == L - 1) ? 0 : y + 1;
-            const T south = act ? src[(long long)ys * L + x] : T(0);
-            T west = __shfl_up_sync(0xffffffffu, cur, 1);
-            T east = __shfl_down_sync(0xffffffffu, cur, 1);
-            if (lane == 0) west = src[(long long)y * L + xw];
-            if (lane == w - 1) east = src[(long long)y * L + xe];
-            const T nsum = ((north + south) + west) + east;
-            const T alpha = A.dcoef * nsum;
-            const bool live = act && !(alpha == T(0) && cur == T(0)) && SAMP != 2;
-            if (!live) Wres[r * 32 + lane] = (SAMP == 2 && act) ? a1 * cur + a2 * alpha : T(0);
-            const unsigned bal = __ballot_sync(0xffffffffu, live);
-            if (live) {
-                const int pos = nq + __popc(bal & lt_mask);
-                Wqi[pos] = (unsigned short)(r * 32 + lane);
-                Wqm[pos] = pm * cur;
-                Wqmu[pos] = alpha * A.two_s2;
-            }
-            nq += __popc(bal);
-            north = cur;
-            cur = south;
-        }
-        __syncwarp();
-        // pass 2: every lane draws for queued sites until the queue is empty.  FP32
-        // takes the straight-line common case first and compacts the rest into a
-        // second queue drawn with the general sampler (same stream, same bits).
-        unsigned st = 0;
-        const unsigned long long seed = A.it.seed[k];
-        int ndef = 0;
-        if constexpr (sizeof(T) == 4) {
-            for (int base = 0; base < nq; base += 32) {
-                const int j = base + lane;
-                const bool has = j < nq;
-                bool deferred = false;
-                if (has) {
-                    const int li = Wqi[j];
-                    const int site = (y0 + (li >> 5)) * L + x0 + (li & 31);
-                    const float v = dornic_draw_fast(seed, (uint32_t)site, step, Wqm[j], Wqmu[j], inv_lambda,
-                                                     SAMP, tab, deferred);
-                    if (!deferred) Wres[li] = v;
-                }
-                const unsigned bal = __ballot_sync(0xffffffffu, has && deferred);
-                if (has && deferred) Wdef[ndef + __popc(bal & lt_mask)] = (unsigned short)j;
-                ndef += __popc(bal);
-            }
-            __syncwarp();
-        } else {
-            for (int j = lane; j < nq; j += 32) Wdef[j] = (unsigned short)j;
-            ndef = nq;
-            __syncwarp();
-        }
-        for (int jj = lane; jj < ndef; jj += 32) {
-            const int j = Wdef[jj];
-            const int li = Wqi[j];
-            const int site = (y0 + (li >> 5)) * L + x0 + (li & 31);
-            Stream<T> g;
-            g.init(seed, (uint32_t)site, step);
-            Wres[li] = dornic_draw(g, Wqm[j], Wqmu[j], inv_lambda, SAMP, tab);
-            st |= g.status;
-        }
-        __syncwarp();
-        // pass 3: remainder, clamp, store
-        if (act) {
-            const T* __restrict__ sb = A.site_b ? A.site_b + A.it.off[k] : nullptr;
+    int nc = 0;  // entries carried in Ck/Cs/Cm/Cmu
+    // One more trip after the last task draws the carried entries; the general
+    // sampler has a single call site, so its code is in the loop body once.
+    for (int t = gw;; t += nw) {
+        const bool more = t < A.n_tasks;
+        int k = 0, L = 0, x0 = 0, y0 = 0, ndef = 0;
+        if (more) k = A.tasks[t].x;
+        if (more && (A.it.alive == nullptr || A.it.alive[k] != 0)) {
+            const int4 tk = A.tasks[t];
+            L = A.it.L[k];
+            const T* __restrict__ src = A.in + A.it.off[k];
+            T* __restrict__ dst = A.out + A.it.off[k];
+            const Dc4 cs = A.it.consts[k];
+            const T pm = (T)cs.x, inv_lambda = (T)cs.y, a1 = (T)cs.z, a2 = (T)cs.w;
+            x0 = tk.y;
+            y0 = tk.z;
+            const int rows = tk.w;
+            const int w = min(32, L - x0);
+            const int x = x0 + lane;
+            const bool act = lane < w;
+            const int xw = (x0 == 0) ? L - 1 : x0 - 1;
+            const int xe = (x0 + w == L) ? 0 : x0 + w;
+            const int yn = (y0 == 0) ? L - 1 : y0 - 1;
+            // pass 1: stream the rows, form alpha_i, resolve absorbing sites and the
+            // noise-off mean directly, queue the live sites (row-major order)
+            T north = act ? src[(long long)yn * L + x] : T(0);
+            T cur = act ? src[(long long)y0 * L + x] : T(0);
+            int nq = 0;
+            unsigned drows = 0;  // rows of this lane's column left to the general sampler
+            Wrows[lane] = 0u;
             for (int r = 0; r < rows; ++r) {
-                const T rs = Wres[r * 32 + lane];
-                const T bi = sb ? sb[(long long)(y0 + r) * L + x] : A.b;
-                T res;
-                if (REM == 0) {
-                    res = rs / (T(1) + (bi * rs) * A.dt);
-                } else if (REM == 1) {
-                    const T k1 = rem_f(rs, bi, A.c, A.cubic);
-                    const T k2 = rem_f(rs + A.dt2 * k1, bi, A.c, A.cubic);
-                    const T k3 = rem_f(rs + A.dt2 * k2, bi, A.c, A.cubic);
-                    const T k4 = rem_f(rs + A.dt * k3, bi, A.c, A.cubic);
-                    res = rs + A.dt6 * (((k1 + T(2) * k2) + T(2) * k3) + k4);
+                const int y = y0 + r;
+                const int ys = (y == L - 1) ? 0 : y + 1;
+                const T south = act ? src[(long long)ys * L + x] : T(0);
+                T west = __shfl_up_sync(0xffffffffu, cur, 1);
+                T east = __shfl_down_sync(0xffffffffu, cur, 1);
+                if (lane == 0) west = src[(long long)y * L + xw];
+                if (lane == w - 1) east = src[(long long)y * L + xe];
+                const T nsum = ((north + south) + west) + east;
+                const T alpha = A.dcoef * nsum;
+                const bool live = act && !(alpha == T(0) && cur == T(0)) && SAMP != 2;
+                if (!live) Wres[r * 32 + lane] = (SAMP == 2 && act) ? a1 * cur + a2 * alpha : T(0);
+                if (sizeof(T) == 8 && live) drows |= 1u << r;
+                const unsigned bal = __ballot_sync(0xffffffffu, live);
+                if (live) {
+                    const int pos = nq + __popc(bal & lt_mask);
+                    Wqi[pos] = (unsigned short)(r * 32 + lane);
+                    Wqm[pos] = pm * cur;
+                    Wqmu[pos] = alpha * A.two_s2;
+                }
+                nq += __popc(bal);
+                north = cur;
+                cur = south;
+            }
+            __syncwarp();
+            // pass 2: FP32 takes the straight-line common case for every queued
+            // site and lists the rest for the general sampler (same stream, same
+            // bits); FP64 lists every queued site.
+            const unsigned long long seed = A.it.seed[k];
+            if constexpr (sizeof(T) == 4) {
+                for (int base = 0; base < nq; base += 32) {
+                    const int j = base + lane;
+                    const bool has = j < nq;
+                    bool deferred = false;
+                    if (has) {
+                        const int li = Wqi[j];
+                        const int site = (y0 + (li >> 5)) * L + x0 + (li & 31);
+                        const float v = dornic_draw_fast(seed, (uint32_t)site, step, Wqm[j], Wqmu[j], inv_lambda,
+                                                         SAMP, tab, deferred);
+                        if (deferred) atomicOr(Wrows + (li & 31), 1u << (li >> 5));
+                        else Wres[li] = v;
+                    }
+                    const unsigned bal = __ballot_sync(0xffffffffu, has && deferred);
+                    if (has && deferred) Wdef[ndef + __popc(bal & lt_mask)] = (unsigned short)j;
+                    ndef += __popc(bal);
+                }
+                __syncwarp();
+                drows = Wrows[lane];
+            } else {
+                for (int j = lane; j < nq; j += 32) Wdef[j] = (unsigned short)j;
+                ndef = nq;
+                __syncwarp();
+            }
+            // pass 3: remainder, clamp, store (sites left to the general sampler
+            // are finished and stored by it)
+            unsigned st = 0;
+            if (act) {
+                const T* __restrict__ sb = A.site_b ? A.site_b + A.it.off[k] : nullptr;
+                for (int r = 0; r < rows; ++r) {
+                    if ((drows >> r) & 1u) continue;
+                    const T bi = sb ? sb[(long long)(y0 + r) * L + x] : A.b;
+                    dst[(long long)(y0 + r) * L + x] = finish_site<T, REM>(A, Wres[r * 32 + lane], bi, st);
+                }
+            }
+            if (st) atomicOr(A.it.status + k, st);
+        }
+        // general sampler: the carried sites, then this task's list, 32 per
+        // pass so that every lane draws; fewer than 32 are carried on (all of
+        // them on the trip after the last task)
+        const int tot = nc + ndef;
+        const int lim = more ? (tot & ~31) : tot;
+        for (int done = 0; done < lim; done += 32) {
+            const int e = done + lane;
+            if (e < lim) {
+                int ke = k;
+                uint32_t se;
+                T me, mue;
+                if (e < nc) {
+                    ke = Ck[e];
+                    se = Cs[e];
+                    me = Cm[e];
+                    mue = Cmu[e];
                 } else {
-                    res = rs;
+                    const int j = Wdef[e - nc];
+                    const int li = Wqi[j];
+                    se = (uint32_t)((y0 + (li >> 5)) * L + x0 + (li & 31));
+                    me = Wqm[j];
+                    mue = Wqmu[j];
                 }
-                if (REM != 2) {
-                    if (res < A.ceps && res >= A.clo) res = T(0);
-                    st |= value_status(res);
-                }
-                dst[(long long)(y0 + r) * L + x] = res;
+                draw_general_site<T, REM, SAMP>(A, tab, step, ke, se, me, mue);
             }
         }
+        if (!more) break;
         __syncwarp();
-        if (st) atomicOr(A.it.status + k, st);
+        const int left = tot - lim;
+        // a carried entry that is still left keeps its slot (lim == 0, e == lane)
+        if (lane < left && lim + lane >= nc) {
+            const int j = Wdef[lim + lane - nc];
+            const int li = Wqi[j];
+            Ck[lane] = k;
+            Cs[lane] = (uint32_t)((y0 + (li >> 5)) * L + x0 + (li & 31));
+            Cm[lane] = Wqm[j];
+            Cmu[lane] = Wqmu[j];
+        }
+        nc = left;
+        __syncwarp();
     }
 }
 
