@@ -1,19 +1,21 @@
 """Generate the ziggurat tables for the standard normal sampler.
 
 G. Marsaglia and W. W. Tsang, "The Ziggurat Method for Generating Random
-Variables", J. Stat. Software 5(8), 2000: 128 layers of equal area v under
+Variables", J. Stat. Software 5(8), 2000: N = 256 layers of equal area v under
 f(x) = exp(-x^2/2), x >= 0, with the base layer ending at R (the tail beyond R
-is sampled by Marsaglia's exponential method).  Index and value come from
-separate bits of one 32-bit word (index: low 7 bits; value: the signed top 25
-bits), avoiding the index/value correlation Doornik (2005) noted in the
-original.
+is sampled by Marsaglia's exponential method); R and v are the paper's
+256-layer values.  Index and value come from separate bits of one 32-bit word
+(index: low 8 bits; value: the signed top 24 bits), avoiding the index/value
+correlation Doornik (2005) noted in the original.  With 256 layers the fast
+test accepts 98.5 % of draws (97.2 % with 128).
 
-Layer i (1..127) is the rectangle [0, x_i] x [f(x_i), f(x_{i+1})] with
-x_1 = R > x_2 > ... > x_128 = 0; layer 0 is [0, v/f(R)] x [0, f(R)] plus the
-tail.  Tables: K[i] = floor(2^24 * x_{i+1}/x_i) (K[0] = floor(2^24 R f(R)/v)),
-W[i] = x_i / 2^24 (W[0] = v/f(R)/2^24), F[i] = f(x_i) (F[0] = f(R),
-F[128] = 1).  A draw z = hz*W[iz] with |hz| < K[iz] lies in the part of the
-layer under the curve and is accepted at once.
+Layer i (1..255) is the rectangle [0, x_i] x [f(x_i), f(x_{i+1})] with
+x_1 = R > x_2 > ... > x_256 = 0; layer 0 is [0, v/f(R)] x [0, f(R)] plus the
+tail.  Tables, with S = 2^23 the magnitude range of the signed value:
+K[i] = floor(S * x_{i+1}/x_i) (K[0] = floor(S R f(R)/v)), W[i] = x_i / S
+(W[0] = v/f(R)/S), F[i] = f(x_i) (F[0] = f(R), F[256] = 1).  A draw
+z = hz*W[iz] with |hz| < K[iz] lies in the part of the layer under the curve
+and is accepted at once.
 
 Writes oracle/tm_zig_table.inc (used by the oracle) and
 trophic_maelstorm_gb300/csrc/tm_zig_table.cuh (used by the kernels) with the
@@ -26,9 +28,11 @@ import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
-N = 128
-R = 3.442619855899
-V = 9.91256303526217e-3
+N = 256
+BITS = 8                      # log2(N): index bits of the word
+S = 2 ** (31 - BITS)          # magnitude range of the signed value
+R = 3.6541528853610088
+V = 4.92867323399e-3
 
 
 def tables():
@@ -42,12 +46,12 @@ def tables():
     K = [0] * N
     W = [0.0] * N
     F = [0.0] * (N + 1)
-    K[0] = int(math.floor(2 ** 24 * R / xt0))
-    W[0] = xt0 / 2 ** 24
+    K[0] = int(math.floor(S * R / xt0))
+    W[0] = xt0 / S
     F[0] = f(R)
     for i in range(1, N):
-        K[i] = int(math.floor(2 ** 24 * x[i + 1] / x[i]))
-        W[i] = x[i] / 2 ** 24
+        K[i] = int(math.floor(S * x[i + 1] / x[i]))
+        W[i] = x[i] / S
         F[i] = f(x[i])
     F[N] = 1.0
     return K, W, F, x
@@ -62,14 +66,14 @@ def emit():
               f" * (Marsaglia & Tsang 2000), {N} layers, R = {R}, v = {V} */\n")
     with open(os.path.join(HERE, "tm_zig_table.inc"), "w") as fh:
         fh.write(common)
-        fh.write(f"#define TMO_ZIG_R {float(R).hex()}\n")
+        fh.write(f"#define TMO_ZIG_R {float(R).hex()}\n#define TMO_ZIG_BITS {BITS}\n")
         fh.write(f"static const uint32_t tmo_zig_k[{N}] = {{{kl}}};\n")
         fh.write(f"static const double tmo_zig_w[{N}] = {{{wl}}};\n")
         fh.write(f"static const double tmo_zig_f[{N + 1}] = {{{fl}}};\n")
     with open(os.path.join(REPO, "trophic_maelstorm_gb300", "csrc", "tm_zig_table.cuh"), "w") as fh:
         fh.write(common)
         fh.write("#pragma once\n#include <stdint.h>\nnamespace tmg {\n")
-        fh.write(f"constexpr int kZigN = {N};\n")
+        fh.write(f"constexpr int kZigN = {N};\nconstexpr int kZigBits = {BITS};\n")
         fh.write(f"constexpr double kZigR = {float(R).hex()};\n")
         fh.write(f"__device__ const uint32_t kZigK[{N}] = {{{kl}}};\n")
         fh.write(f"__device__ const double kZigW[{N}] = {{{wl}}};\n")
@@ -79,6 +83,7 @@ def emit():
 
 if __name__ == "__main__":
     K, W, F, x = tables()
-    print("x_127 =", x[N - 1], "x_128 set to 0; f(x_127)+v/x_127 =", math.exp(-0.5 * x[N - 1] ** 2) + V / x[N - 1])
-    print("K[0..3]", K[:4], "K[127]", K[127])
+    print(f"x_{N - 1} =", x[N - 1], f"x_{N} set to 0; f(x_{N - 1})+v/x_{N - 1} =",
+          math.exp(-0.5 * x[N - 1] ** 2) + V / x[N - 1])
+    print("K[0..3]", K[:4], f"K[{N - 1}]", K[N - 1], "fast-test acceptance", sum(K) / (N * S))
     emit()

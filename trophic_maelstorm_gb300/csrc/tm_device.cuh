@@ -326,6 +326,15 @@ template <> __device__ __forceinline__ float Stream<float>::open()
     return ((float)(w >> 8) + 0.5f) * 0x1p-24f;
 }
 
+// Ziggurat word split: layer index (low kZigBits bits) and the signed value
+// (the remaining bits, centred on 0).
+__device__ __forceinline__ int zig_layer(uint32_t w) { return (int)(w & (uint32_t)(kZigN - 1)); }
+__device__ __forceinline__ int32_t zig_value(uint32_t w)
+{
+    return (int32_t)(w >> kZigBits) - (int32_t)(1 << (31 - kZigBits));
+}
+static_assert(kZigN == (1 << kZigBits), "ziggurat layer count");
+
 // Tables every sampler reads, staged in shared memory by the kernel:
 // rcp[n] = 1/n (n <= 200) and the ziggurat (K: thresholds, W: widths, F: f(x_i)).
 constexpr int kRcpTable = 201;
@@ -347,7 +356,7 @@ struct SmemTab {
 };
 
 // standard normal by the ziggurat: one 32-bit word per attempt (layer index
-// from the low 7 bits, signed value from the top 25), wedge test or
+// from the low kZigBits bits, signed value from the rest), wedge test or
 // Marsaglia's tail method when the fast test fails.
 template <typename T>
 template <class Tab>
@@ -355,8 +364,8 @@ __device__ __forceinline__ T Stream<T>::normal(const Tab& tb)
 {
     for (int it = 0; it < 64; ++it) {
         const uint32_t w = u32();
-        const int iz = (int)(w & 127u);
-        const int32_t hz = (int32_t)(w >> 7) - (int32_t)(1 << 24);
+        const int iz = zig_layer(w);
+        const int32_t hz = zig_value(w);
         const uint32_t az = (uint32_t)(hz < 0 ? -hz : hz);
         const T x = (T)hz * tb.zw[iz];
         if (az < tb.zk[iz]) return x;
@@ -523,10 +532,10 @@ __device__ __forceinline__ T dornic_draw(Stream<T>& g, T m, T mu1, T inv_lambda,
 // Straight-line draw for the common case (FP32): one Philox block of four
 // words, Poisson by inversion finishing within kFastInv steps, a ziggurat
 // normal accepted by its fast test, one Marsaglia-Tsang attempt accepted by
-// the squeeze and, for shape < 1, the U^(1/k) boost from the next word.  Every step consumes the counter stream exactly as
-// dornic_draw does, so when it returns without deferring the value equals
-// dornic_draw's bit for bit; otherwise (*deferred) the caller recomputes the
-// site with dornic_draw.
+// the squeeze and, for shape < 1, the U^(1/k) boost from the next word.  Every
+// step consumes the counter stream exactly as dornic_draw does, so when it
+// returns without deferring the value equals dornic_draw's bit for bit;
+// otherwise (*deferred) the caller recomputes the site with dornic_draw.
 constexpr int kFastInv = 32;
 static_assert(kFastInv % 4 == 0, "the inversion takes four terms per trip");
 
@@ -542,15 +551,15 @@ __device__ __forceinline__ float dornic_draw_fast(uint64_t seed, uint32_t site, 
     if (sampler == 1 && m > 100.0f) {
         // Gaussian approximations of both draws (multiSPDP.cpp:2922-2943): one
         // ziggurat word each
-        const int i1 = (int)(r.x & 127u);
-        const int32_t h1 = (int32_t)(r.x >> 7) - (int32_t)(1 << 24);
+        const int i1 = zig_layer(r.x);
+        const int32_t h1 = zig_value(r.x);
         const uint32_t a1 = (uint32_t)(h1 < 0 ? -h1 : h1);
         if (!(a1 < tb.zk[i1])) { deferred = true; return 0.0f; }
         const float z1 = (float)h1 * tb.zw[i1];
         const float kk = mu1 + truncf(z1 * sqrtf(m) + m);
         if (!(kk > 100.0f)) { deferred = true; return 0.0f; }
-        const int i2 = (int)(r.y & 127u);
-        const int32_t h2 = (int32_t)(r.y >> 7) - (int32_t)(1 << 24);
+        const int i2 = zig_layer(r.y);
+        const int32_t h2 = zig_value(r.y);
         const uint32_t a2 = (uint32_t)(h2 < 0 ? -h2 : h2);
         if (!(a2 < tb.zk[i2])) { deferred = true; return 0.0f; }
         const float z2 = (float)h2 * tb.zw[i2];
@@ -593,8 +602,8 @@ __device__ __forceinline__ float dornic_draw_fast(uint64_t seed, uint32_t site, 
     const float kk = boost ? k + 1.0f : k;
     const float d = kk - (float)(1.0 / 3.0);
     const float c = 1.0f / sqrtf(9.0f * d);
-    const int iz = (int)(wz & 127u);
-    const int32_t hz = (int32_t)(wz >> 7) - (int32_t)(1 << 24);
+    const int iz = zig_layer(wz);
+    const int32_t hz = zig_value(wz);
     const uint32_t az = (uint32_t)(hz < 0 ? -hz : hz);
     if (!(az < tb.zk[iz])) { deferred = true; return 0.0f; }
     const float x = (float)hz * tb.zw[iz];
