@@ -92,6 +92,21 @@ int ref_libstdcxx_draws(int kind, double param, unsigned long long seed, int n, 
     return n;
 }
 
+// The whole draw of the reference's Dornic step (stochasticSPDP.cpp:1053-1059):
+// a libstdc++ Poisson count of mean m, then a libstdc++ Gamma of shape mu1 plus
+// that count, both from one seeded mt19937_64 (the scale 1/lambda left out).
+int ref_libstdcxx_dornic(double m, double mu1, unsigned long long seed, int n, double* out)
+{
+    std::mt19937_64 rng(seed);
+    for (int i = 0; i < n; ++i) {
+        std::poisson_distribution<int> pd(m);
+        const int count = pd(rng);
+        std::gamma_distribution<double> gd(mu1 + count, 1.0);
+        out[i] = gd(rng);
+    }
+    return n;
+}
+
 int ref_logarithm10_time_bins(double t_max, double dt, double* out, int max_n)
 {
     Mute m;

@@ -22,7 +22,8 @@ ref_dp_ensemble.npz  per-replicate trajectories of percolationDornic_2D
                    the reference's ensemble, compared statistically.
 ref_libstdcxx.npz  draws of the libstdc++ poisson_distribution / gamma_distribution
                    the reference's Dornic step constructs (stochasticSPDP.cpp:1055-1059),
-                   from a seeded std::mt19937_64.
+                   from a seeded std::mt19937_64, alone and composed as the step's whole
+                   draw Gamma(mu1 + Poisson(m)).
 
     python tests/golden/gen_golden.py --fke        # only ref_fke.npz
     python tests/golden/gen_golden.py --libstdcxx  # only ref_libstdcxx.npz
@@ -65,6 +66,7 @@ def load(names=("dp", "rietkerk", "multisp")):
     d.ref_rk4_first_order.argtypes = [dp, C.c_int] + [C.c_double] * 7
     d.ref_logarithm10_time_bins.argtypes = [C.c_double, C.c_double, dp, C.c_int]
     d.ref_libstdcxx_draws.argtypes = [C.c_int, C.c_double, C.c_ulonglong, C.c_int, dp]
+    d.ref_libstdcxx_dornic.argtypes = [C.c_double, C.c_double, C.c_ulonglong, C.c_int, dp]
     if "rietkerk" not in libs:
         return libs
     r = libs["rietkerk"]
@@ -199,6 +201,9 @@ def fke(libs, rng):
 # means and shapes of the sampler-level comparison with libstdc++
 LIBSTDCXX_POISSON = (0.3, 3.0, 17.0, 50.0, 250.0)
 LIBSTDCXX_GAMMA = (0.4, 1.7, 8.0, 60.0)
+# (m, mu1) of the whole-draw comparison, from the dilute to the dense regime
+LIBSTDCXX_DORNIC = ((16.7, 6.0), (4.0, 1.5), (3.9, 1.5), (8.0, 1.4), (8.0, 2.0), (50.0, 12.0), (2.0, 0.8),
+                    (120.0, 40.0))
 LIBSTDCXX_N = 6000
 
 
@@ -211,8 +216,13 @@ def libstdcxx(libs):
             x = np.zeros(LIBSTDCXX_N)
             libs["dp"].ref_libstdcxx_draws(kind, v, 1000 + 17 * k + kind, LIBSTDCXX_N, _p(x))
             out[f"{'poisson' if kind == 0 else 'gamma'}_{k}"] = x.astype(np.float32)
+    for k, (m, mu1) in enumerate(LIBSTDCXX_DORNIC):
+        x = np.zeros(LIBSTDCXX_N)
+        libs["dp"].ref_libstdcxx_dornic(m, mu1, 5000 + 31 * k, LIBSTDCXX_N, _p(x))
+        out[f"dornic_{k}"] = x.astype(np.float32)
     out["poisson_params"] = np.array(LIBSTDCXX_POISSON)
     out["gamma_params"] = np.array(LIBSTDCXX_GAMMA)
+    out["dornic_params"] = np.array(LIBSTDCXX_DORNIC)
     return out
 
 

@@ -86,7 +86,7 @@ def test_determinism_and_precision_consistency(oracle):
 
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
 @pytest.mark.parametrize("m,mu1", [(16.7, 6.0), (3.0, 0.9), (0.2, 0.55), (50.0, 1.2), (7.0, 0.3), (0.05, 0.1),
-                                   (250.0, 30.0)])
+                                   (250.0, 30.0), (30.0, 100.0)])
 def test_dornic_draw_law(oracle, dtype, m, mu1):
     """The whole Dornic draw against its exact law: for X = Gamma(mu1 + Poisson(m)), 2X is
     noncentral chi-square with 2 mu1 degrees of freedom and noncentrality 2m (KS p > 1e-3),
@@ -128,3 +128,17 @@ def test_gamma_matches_libstdcxx(oracle, dtype):
         x, st = oracle.sample("gamma", len(ref), seed=57 + k, k=float(shape), dtype=dtype)
         assert st == 0
         assert stats.ks_2samp(x.astype(np.float64), ref).pvalue > 1e-3, shape
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_dornic_draw_matches_libstdcxx(oracle, dtype):
+    """The oracle's whole Dornic draw against the reference's own: a libstdc++ Poisson count,
+    then a libstdc++ Gamma of shape mu1 + count (stochasticSPDP.cpp:1053-1059).  Two-sample KS,
+    p > 1e-3, from the dilute to the dense regime and across the inversion/PTRS switch."""
+    z = _libstdcxx()
+    for k, (m, mu1) in enumerate(z["dornic_params"]):
+        ref = z[f"dornic_{k}"].astype(np.float64)
+        x, st = oracle.sample("dornic", len(ref), seed=71 + k, m=float(m), mu1=float(mu1), inv_lambda=1.0,
+                              dtype=dtype)
+        assert st == 0
+        assert stats.ks_2samp(x.astype(np.float64), ref).pvalue > 1e-3, (m, mu1)
