@@ -175,12 +175,16 @@ DornicArgs<T> dornic_args(const tm_batch* b, const T* in, T* out, const long lon
         a.b = (T)m.b; a.c = (T)m.c; a.dt = (T)m.dt; a.dt2 = (T)(m.dt / 2.0); a.dt6 = (T)(m.dt / 6.0);
         a.clo = (T)m.clamp_lo; a.ceps = (T)m.clamp_eps;
         a.sampler = m.sampler; a.cubic = (m.c != 0.0);
+        // the remainder and the clamp map +0 to +0 whenever these are finite
+        a.zero_fixed = a.site_b == nullptr && std::isfinite(a.b) && std::isfinite(a.c) && std::isfinite(a.dt) &&
+                       std::isfinite(a.dt2) && std::isfinite(a.dt6);
     } else {
         const tm_rietkerk_model& m = b->rkm;
         a.dcoef = (T)(m.DP / (m.dx * m.dx));
         a.two_s2 = (T)(2.0 / (m.sigma * m.sigma));
         a.sampler = m.sampler;
         a.it.alive = nullptr;
+        a.zero_fixed = 1;  // no remainder, no clamp
     }
     return a;
 }

@@ -45,6 +45,7 @@ struct DornicArgs {
     int cubic;
     int rows_cap;                  // rows of the largest task (<= kMaxRowsPerTask)
     const T* site_b;               // per-site loss coefficient b_v (packed like the state) or nullptr
+    int zero_fixed;                // a +0 draw finishes as +0, no status bit (finite b, c, dt; no site_b)
 };
 
 template <typename T>

@@ -86,8 +86,8 @@ __global__ void __launch_bounds__(RK_THREADS, 3) rk4_tile_kernel(const RK4Args<T
     T* const X0 = reinterpret_cast<T*>(rk_smem);          // [3][RK_RN] stage-0 input
     T* const MA = X0 + 3 * RK_RN;                           // [3][RK_RN] stage inputs (ping)
     T* const MB = MA + 3 * RK_RN;                           // [3][RK_RN] (pong)
-    T* const ACC = MB + 3 * RK_RN;                          // [3][RK_TX*RK_TY] weighted sum of K
-    constexpr int NI = RK_TX * RK_TY;
+    constexpr int kPer = RK_TX * RK_TY / RK_THREADS;        // interior cells per thread
+    static_assert(RK_TX * RK_TY % RK_THREADS == 0, "interior cells per thread");
     const int tid = threadIdx.x;
     const uint32_t bar = rk_saddr(&tile_bar);
     if (tid == 0) {
@@ -169,31 +169,55 @@ __global__ void __launch_bounds__(RK_THREADS, 3) rk4_tile_kernel(const RK4Args<T
             X0[2 * RK_RN + c] = O0[gi];
         }
         __syncthreads();
+        // Stage s on the region inset by s+1: the 64 x 16 interior with a fixed
+        // thread mapping (kPer cells per thread, whose weighted sums of K stay in
+        // registers), then the ring between the inset and the interior.
+        T acc[3][kPer];
 #pragma unroll
         for (int s = 0; s < 4; ++s) {
             const T* S = (s == 0) ? X0 : ((s & 1) ? MA : MB);
             T* D = (s & 1) ? MB : MA;
             const T coef = (s == 2) ? A.dt : A.dt2;
-            const int in = s + 1;
-            const int w = RK_RX - 2 * in, h = RK_RY - 2 * in;
-            for (int q = tid; q < w * h; q += RK_THREADS) {
-                const int ry = in + q / w, rx = in + q % w;
-                const int c = ry * RK_RX + rx;
+#pragma unroll
+            for (int j = 0; j < kPer; ++j) {
+                const int a = tid + j * RK_THREADS;
+                const int c = ((a / RK_TX) + RK_H) * RK_RX + (a % RK_TX) + RK_H;
                 T k0, k1, k2;
                 rk_rhs_cell<T, DET>(A, S, c, R, k0, k1, k2);
-                const int ly = ry - RK_H, lx = rx - RK_H;
-                if (ly >= 0 && ly < RK_TY && lx >= 0 && lx < RK_TX) {
-                    const int a = ly * RK_TX + lx;
-                    if (s == 0) {
-                        ACC[a] = k0; ACC[NI + a] = k1; ACC[2 * NI + a] = k2;
-                    } else if (s == 3) {
-                        ACC[a] = ACC[a] + k0; ACC[NI + a] = ACC[NI + a] + k1; ACC[2 * NI + a] = ACC[2 * NI + a] + k2;
-                    } else {
-                        ACC[a] = ACC[a] + T(2) * k0; ACC[NI + a] = ACC[NI + a] + T(2) * k1;
-                        ACC[2 * NI + a] = ACC[2 * NI + a] + T(2) * k2;
-                    }
+                if (s == 0) {
+                    acc[0][j] = k0; acc[1][j] = k1; acc[2][j] = k2;
+                } else if (s == 3) {
+                    acc[0][j] = acc[0][j] + k0; acc[1][j] = acc[1][j] + k1; acc[2][j] = acc[2][j] + k2;
+                } else {
+                    acc[0][j] = acc[0][j] + T(2) * k0; acc[1][j] = acc[1][j] + T(2) * k1;
+                    acc[2][j] = acc[2][j] + T(2) * k2;
                 }
                 if (s < 3) {
+                    D[c] = X0[c] + coef * k0;
+                    D[RK_RN + c] = X0[RK_RN + c] + coef * k1;
+                    D[2 * RK_RN + c] = X0[2 * RK_RN + c] + coef * k2;
+                }
+            }
+            if (s < 3) {
+                // ring of thickness t = 3 - s: top and bottom bands (t rows of the
+                // inset's width w), then left and right bands (RK_TY rows, t columns)
+                const int in = s + 1, t = 3 - s, w = RK_RX - 2 * in;
+                const int nband = t * w, nside = RK_TY * t;
+                for (int q = tid; q < 2 * nband + 2 * nside; q += RK_THREADS) {
+                    int ry, rx;
+                    if (q < 2 * nband) {
+                        const int qb = q < nband ? q : q - nband;
+                        ry = (q < nband ? in : RK_H + RK_TY) + qb / w;
+                        rx = in + qb % w;
+                    } else {
+                        const int qs = q - 2 * nband;
+                        const int qq = qs < nside ? qs : qs - nside;
+                        ry = RK_H + qq / t;
+                        rx = (qs < nside ? in : RK_H + RK_TX) + qq % t;
+                    }
+                    const int c = ry * RK_RX + rx;
+                    T k0, k1, k2;
+                    rk_rhs_cell<T, DET>(A, S, c, R, k0, k1, k2);
                     D[c] = X0[c] + coef * k0;
                     D[RK_RN + c] = X0[RK_RN + c] + coef * k1;
                     D[2 * RK_RN + c] = X0[2 * RK_RN + c] + coef * k2;
@@ -202,15 +226,17 @@ __global__ void __launch_bounds__(RK_THREADS, 3) rk4_tile_kernel(const RK4Args<T
             __syncthreads();
         }
         unsigned st = 0;
-        for (int a = tid; a < NI; a += RK_THREADS) {
-            const int ly = a / RK_TX, lx = a - ly * RK_TX;
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            const int a = tid + j * RK_THREADS;
+            const int ly = a / RK_TX, lx = a % RK_TX;
             const int gy = y0 + ly, gx = x0 + lx;
             if (gy < L && gx < L) {
                 const int c = (ly + RK_H) * RK_RX + lx + RK_H;
                 const long long gi = off + (long long)gy * L + gx;
 #pragma unroll
                 for (int f = 0; f < 3; ++f) {
-                    T v = X0[f * RK_RN + c] + A.dt6 * ACC[f * NI + a];
+                    T v = X0[f * RK_RN + c] + A.dt6 * acc[f][j];
                     if (v < A.ceps && v >= A.clo) v = T(0);
                     st |= value_status(v);
                     A.out[gi + f * fs] = v;
@@ -225,7 +251,7 @@ template <typename T>
 cudaError_t launch_rk4(const RK4Args<T>& a, bool det, int grid, cudaStream_t s)
 {
     if (a.n_tasks <= 0) return cudaSuccess;
-    const size_t smem = (9 * (size_t)RK_RN + 3 * (size_t)RK_TX * RK_TY) * sizeof(T);
+    const size_t smem = 9 * (size_t)RK_RN * sizeof(T);
     static bool attr[2] = {false, false};
     cudaError_t e = cudaSuccess;
     if (!attr[det ? 1 : 0]) {

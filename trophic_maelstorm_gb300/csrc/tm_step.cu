@@ -44,6 +44,9 @@ __host__ __device__ __forceinline__ size_t warp_scratch_bytes(int rows_cap)
     return (size_t)rows_cap * 32 * (3 * sizeof(T) + 2 * sizeof(unsigned short)) + 32 * (2 * sizeof(T) + 8);
 }
 
+__device__ __forceinline__ bool is_pos_zero(float x) { return __float_as_uint(x) == 0u; }
+__device__ __forceinline__ bool is_pos_zero(double x) { return __double_as_longlong(x) == 0LL; }
+
 // Remainder, clamp and status bits of one site after its Dornic draw.
 template <typename T, int REM>
 __device__ __forceinline__ T finish_site(const DornicArgs<T>& A, T rs, T bi, unsigned& st)
@@ -136,25 +139,38 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
             const int yn = (y0 == 0) ? L - 1 : y0 - 1;
             // pass 1: stream the rows, form alpha_i, resolve absorbing sites and the
             // noise-off mean directly, queue the live sites (row-major order)
+            // the strip-edge columns of the task's rows, one row per lane; the
+            // column itself is read one row ahead of its use
+            const bool erow = lane < rows;
+            const T wcol = erow ? src[(long long)(y0 + lane) * L + xw] : T(0);
+            const T ecol = erow ? src[(long long)(y0 + lane) * L + xe] : T(0);
             T north = act ? src[(long long)yn * L + x] : T(0);
             T cur = act ? src[(long long)y0 * L + x] : T(0);
+            T south = act ? src[(long long)((y0 == L - 1) ? 0 : y0 + 1) * L + x] : T(0);
             int nq = 0;
             unsigned drows = 0;  // rows of this lane's column left to the general sampler
             Wrows[lane] = 0u;
             for (int r = 0; r < rows; ++r) {
                 const int y = y0 + r;
-                const int ys = (y == L - 1) ? 0 : y + 1;
-                const T south = act ? src[(long long)ys * L + x] : T(0);
+                T next = T(0);
+                if (r + 1 < rows) {
+                    int y2 = y + 2;
+                    if (y2 >= L) y2 -= L;
+                    if (y2 >= L) y2 -= L;
+                    next = act ? src[(long long)y2 * L + x] : T(0);
+                }
                 T west = __shfl_up_sync(0xffffffffu, cur, 1);
                 T east = __shfl_down_sync(0xffffffffu, cur, 1);
-                if (lane == 0) west = src[(long long)y * L + xw];
-                if (lane == w - 1) east = src[(long long)y * L + xe];
+                const T wedge = __shfl_sync(0xffffffffu, wcol, r);
+                const T eedge = __shfl_sync(0xffffffffu, ecol, r);
+                if (lane == 0) west = wedge;
+                if (lane == w - 1) east = eedge;
                 const T nsum = ((north + south) + west) + east;
                 const T alpha = A.dcoef * nsum;
                 const bool live = act && !(alpha == T(0) && cur == T(0)) && SAMP != 2;
+                const unsigned bal = __ballot_sync(0xffffffffu, live);
                 if (!live) Wres[r * 32 + lane] = (SAMP == 2 && act) ? a1 * cur + a2 * alpha : T(0);
                 if (sizeof(T) == 8 && live) drows |= 1u << r;
-                const unsigned bal = __ballot_sync(0xffffffffu, live);
                 if (live) {
                     const int pos = nq + __popc(bal & lt_mask);
                     Wqi[pos] = (unsigned short)(r * 32 + lane);
@@ -164,6 +180,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
                 nq += __popc(bal);
                 north = cur;
                 cur = south;
+                south = next;
             }
             __syncwarp();
             // pass 2: FP32 takes the straight-line common case for every queued
@@ -195,14 +212,20 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
                 __syncwarp();
             }
             // pass 3: remainder, clamp, store (sites left to the general sampler
-            // are finished and stored by it)
+            // are finished and stored by it).  When zero_fixed holds a +0 draw --
+            // every absorbing site -- finishes as +0 and skips the arithmetic.
             unsigned st = 0;
             if (act) {
                 const T* __restrict__ sb = A.site_b ? A.site_b + A.it.off[k] : nullptr;
                 for (int r = 0; r < rows; ++r) {
                     if ((drows >> r) & 1u) continue;
-                    const T bi = sb ? sb[(long long)(y0 + r) * L + x] : A.b;
-                    dst[(long long)(y0 + r) * L + x] = finish_site<T, REM>(A, Wres[r * 32 + lane], bi, st);
+                    const T rs = Wres[r * 32 + lane];
+                    T res = rs;
+                    if (!(A.zero_fixed && is_pos_zero(rs))) {
+                        const T bi = sb ? sb[(long long)(y0 + r) * L + x] : A.b;
+                        res = finish_site<T, REM>(A, rs, bi, st);
+                    }
+                    dst[(long long)(y0 + r) * L + x] = res;
                 }
             }
             if (st) atomicOr(A.it.status + k, st);
