@@ -250,7 +250,7 @@ cudaError_t enqueue_step_t(tm_batch* b, int src_idx, const long long* step_base,
         return launch_dornic<T>(a, m.remainder == TM_REM_RK4 ? 1 : 0, warp_grid(b, b->n_tasks), 256, s);
     }
     const tm_rietkerk_model& m = b->rkm;
-    const int grid_rk = std::max(1, std::min(b->n_btasks, b->ctx->num_sms * 3));
+    const int grid_rk = std::max(1, std::min(b->n_btasks, b->ctx->num_sms * RK_CTAS));
     if (m.deterministic) {
         RK4Args<T> r = rk4_args<T>(b, in, nullptr, out);
         return launch_rk4<T>(r, true, grid_rk, s);

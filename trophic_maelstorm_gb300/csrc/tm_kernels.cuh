@@ -88,8 +88,9 @@ cudaError_t launch_det_final(const T* x0, const T* k1, const T* k2, const T* k3,
                              T dt, T dt6, int rk4, cudaStream_t s);
 
 constexpr int kMaxRowsPerTask = 16;
-constexpr int RK_TX = 64, RK_TY = 16, RK_H = 4;
+constexpr int RK_TX = 64, RK_TY = 32, RK_H = 4;
 constexpr int RK_RX = RK_TX + 2 * RK_H, RK_RY = RK_TY + 2 * RK_H, RK_RN = RK_RX * RK_RY;
-constexpr int RK_THREADS = 256;
+constexpr int RK_THREADS = 512;
+constexpr int RK_CTAS = 2;                 // resident RK4 tile CTAs per SM (FP32)
 
 }  // namespace tmg

@@ -4,10 +4,10 @@
 // Rietkerk (rietkerk_bjork_FKE.cpp:2363-2444 stochastic remainder f_2Dor,
 // :1760-1856 noise-off f_2D): the W and O tendencies carry 5-point
 // Laplacians, so stage s needs stage s-1 values one site further out.  A CTA
-// loads a (64+8) x (16+8) region of [P*, W, O] (halo 4, periodic wrap) into
+// loads a (64+8) x (32+8) region of [P*, W, O] (halo 4, periodic wrap) into
 // shared memory and runs all four stages there, stage s only on the region
-// inset by s+1 cells, so the 64 x 16 interior comes out exact after stage 4
-// with 1.25 stage evaluations per cell and stage.
+// inset by s+1 cells, so the 64 x 32 interior comes out exact after stage 4
+// with 1.15 stage evaluations per cell and stage.
 // The state is read and written once per step (plus the halo re-read, which
 // hits L2); the K1..K4 temporaries the reference keeps as full lattices
 // never leave the SM.
@@ -78,7 +78,7 @@ __device__ __forceinline__ bool rk_bar_wait(uint32_t bar, uint32_t parity)
 }
 
 template <typename T, bool DET>
-__global__ void __launch_bounds__(RK_THREADS, 3) rk4_tile_kernel(const RK4Args<T> A)
+__global__ void __launch_bounds__(RK_THREADS, (sizeof(T) == 4 ? RK_CTAS : 1)) rk4_tile_kernel(const RK4Args<T> A)
 {
     extern __shared__ __align__(16) unsigned char rk_smem[];
     __shared__ __align__(8) uint64_t tile_bar;
@@ -169,7 +169,7 @@ __global__ void __launch_bounds__(RK_THREADS, 3) rk4_tile_kernel(const RK4Args<T
             X0[2 * RK_RN + c] = O0[gi];
         }
         __syncthreads();
-        // Stage s on the region inset by s+1: the 64 x 16 interior with a fixed
+        // Stage s on the region inset by s+1: the 64 x 32 interior with a fixed
         // thread mapping (kPer cells per thread, whose weighted sums of K stay in
         // registers), then the ring between the inset and the interior.
         T acc[3][kPer];
