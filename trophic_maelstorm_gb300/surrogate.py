@@ -252,7 +252,13 @@ class Surrogate:
 class Judge:
     """Full simulations that decide on which side of the transition a value of a
     lies: delta_eff of n_rep replicates at lattice side L between t1 and t_max,
-    against delta_DP.  Results are cached per a; `runs` counts the simulations."""
+    against delta_DP.  Results are cached per a; `runs` counts the simulations.
+
+    Common random numbers: replicate j has the same key (initial field and
+    Philox stream) at every a, so two values of a differ by the control
+    parameter only, not by independent sampling noise.  delta_eff(a) is then a
+    smooth function of a for a given judge, and every search that asks the
+    same judge (or one with the same seed) sees the same crossing."""
 
     def __init__(self, ctx, L, n_rep, t_max, t1, seed=7):
         self.ctx, self.L, self.n_rep, self.t_max, self.t1, self.seed = ctx, L, n_rep, t_max, t1, seed
@@ -261,12 +267,12 @@ class Judge:
         self.seconds = 0.0
 
     def _seed(self, a):
-        return self.seed + int(round(a * 1e6)) * 64
+        return self.seed
 
     def delta(self, a_values):
         a_values = [round(float(a), 9) for a in a_values]
         todo = [a for a in dict.fromkeys(a_values) if a not in self.cache]
-        if todo:            # one batch; each value's runs are keyed by the value alone
+        if todo:            # one batch; replicate j has the same key at every value
             e = run_ensembles(self.ctx, todo, self.L, self.n_rep, self.t_max,
                               point_seeds=[self._seed(a) for a in todo])
             i1 = int(np.argmin(np.abs(e.t - self.t1)))
