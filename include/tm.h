@@ -169,8 +169,10 @@ int tm_batch_advance(tm_batch* b, int64_t n_steps, const int64_t* meas_steps, in
 int tm_batch_enqueue_steps(tm_batch* b, int64_t n_steps);
 
 /* Launch shape of the step kernels: rows per warp task (DP/Dornic) and CTAs
- * per SM of the persistent grid.  0 keeps the current value.  tm_batch_autotune
- * times the candidates on the batch itself (state is saved and restored). */
+ * per SM of the persistent grid.  0 keeps the current value.  A new batch
+ * starts at 8 rows (fewer when the batch has too few tasks to fill the GPU) and
+ * 4 CTAs/SM.  tm_batch_autotune times the candidates on the batch itself
+ * (state is saved and restored).  Results do not depend on the launch shape. */
 int tm_batch_set_launch(tm_batch* b, int rows_per_task, int ctas_per_sm);
 int tm_batch_get_launch(const tm_batch* b, int* rows_per_task, int* ctas_per_sm);
 int tm_batch_autotune(tm_batch* b, int steps_per_trial);

@@ -115,6 +115,24 @@ void free_graphs(tm_batch* b)
     }
 }
 
+// Rows per warp task for a new batch: 8, or fewer when the batch is too small
+// to give every scheduler of the GPU two tasks (one 128^2 lattice is 64 tasks of
+// 8 rows).  The results do not depend on the task shape.
+int default_rows(const tm_batch* b)
+{
+    const long long want = 2LL * 4 * std::max(1, b->ctx->num_sms);
+    int R = 8;
+    for (; R > 1; R >>= 1) {
+        long long n = 0;
+        for (int k = 0; k < b->n_inst; ++k) {
+            const long long L = b->inst[k].L;
+            n += ((L + R - 1) / R) * ((L + 31) / 32);
+        }
+        if (n >= want) break;
+    }
+    return R;
+}
+
 int build_tasks(tm_batch* b)
 {
     // warp tasks
@@ -374,6 +392,7 @@ int batch_common_init(tm_batch* b, const tm_instance* inst, int n)
     TM_CUDA(cudaMemcpy(b->d_alive, ones.data(), n * sizeof(int), cudaMemcpyHostToDevice));
     TM_CUDA(cudaMemset(b->d_status, 0, n * sizeof(unsigned)));
     TM_CUDA(cudaMemset(b->d_step, 0, sizeof(long long)));
+    b->rows_per_task = default_rows(b);
     return build_tasks(b);
 }
 
@@ -728,7 +747,7 @@ int tm_batch_autotune(tm_batch* b, int steps_per_trial)
     TM_CUDA(cudaStreamSynchronize(s));
     const int64_t step0 = b->step;
     const int cur0 = b->cur;
-    const int rows_c[] = {4, 8, 16};
+    const int rows_c[] = {1, 2, 4, 8, 16};
     const int ctas_c[] = {1, 2, 3, 4};
     int best_r = b->rows_per_task, best_c = b->ctas_per_sm;
     float best = 1e30f;
