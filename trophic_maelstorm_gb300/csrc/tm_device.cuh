@@ -336,24 +336,30 @@ __device__ __forceinline__ int32_t zig_value(uint32_t w)
 static_assert(kZigN == (1 << kZigBits), "ziggurat layer count");
 
 // Tables every sampler reads, staged in shared memory by the kernel:
-// rcp[n] = 1/n (n <= 200) and the ziggurat (K: thresholds, W: widths, F: f(x_i)).
+// rcp[n] = 1/n (n <= 200) and the ziggurat (K: threshold and W: width of each
+// layer, side by side so that one load reads both; F: f(x_i)).  For FP32, rcp[1]
+// sits on a 16-byte boundary: the straight-line inversion reads rcp[it+1..it+4]
+// with one vector load.
 constexpr int kRcpTable = 201;
 template <typename T>
-struct SmemTab {
+struct ZigLayer {
+    uint32_t k;
+    T w;
+};
+template <typename T>
+struct __align__(16) SmemTab {
+    T pad_[3];
     T rcp[kRcpTable];
-    T zw[kZigN];
+    ZigLayer<T> zig[kZigN];
     T zf[kZigN + 1];
-    uint32_t zk[kZigN];
     __device__ __forceinline__ void fill()
     {
         for (int i = threadIdx.x; i < kRcpTable; i += blockDim.x) rcp[i] = (i == 0) ? T(0) : T(1) / (T)i;
-        for (int i = threadIdx.x; i < kZigN; i += blockDim.x) {
-            zw[i] = (T)kZigW[i];
-            zk[i] = kZigK[i];
-        }
+        for (int i = threadIdx.x; i < kZigN; i += blockDim.x) zig[i] = ZigLayer<T>{kZigK[i], (T)kZigW[i]};
         for (int i = threadIdx.x; i <= kZigN; i += blockDim.x) zf[i] = (T)kZigF[i];
     }
 };
+static_assert(sizeof(ZigLayer<float>) == 8, "one 8-byte load per layer");
 
 // standard normal by the ziggurat: one 32-bit word per attempt (layer index
 // from the low kZigBits bits, signed value from the rest), wedge test or
@@ -367,8 +373,9 @@ __device__ __forceinline__ T Stream<T>::normal(const Tab& tb)
         const int iz = zig_layer(w);
         const int32_t hz = zig_value(w);
         const uint32_t az = (uint32_t)(hz < 0 ? -hz : hz);
-        const T x = (T)hz * tb.zw[iz];
-        if (az < tb.zk[iz]) return x;
+        const ZigLayer<T> zl = tb.zig[iz];
+        const T x = (T)hz * zl.w;
+        if (az < zl.k) return x;
         if (iz == 0) {
             for (int jt = 0; jt < 64; ++jt) {
                 const T xt = -tm_log_pos(open()) * T(1.0 / kZigR);
@@ -554,15 +561,17 @@ __device__ __forceinline__ float dornic_draw_fast(uint64_t seed, uint32_t site, 
         const int i1 = zig_layer(r.x);
         const int32_t h1 = zig_value(r.x);
         const uint32_t a1 = (uint32_t)(h1 < 0 ? -h1 : h1);
-        if (!(a1 < tb.zk[i1])) { deferred = true; return 0.0f; }
-        const float z1 = (float)h1 * tb.zw[i1];
+        const ZigLayer<float> l1 = tb.zig[i1];
+        if (!(a1 < l1.k)) { deferred = true; return 0.0f; }
+        const float z1 = (float)h1 * l1.w;
         const float kk = mu1 + truncf(z1 * sqrtf(m) + m);
         if (!(kk > 100.0f)) { deferred = true; return 0.0f; }
         const int i2 = zig_layer(r.y);
         const int32_t h2 = zig_value(r.y);
         const uint32_t a2 = (uint32_t)(h2 < 0 ? -h2 : h2);
-        if (!(a2 < tb.zk[i2])) { deferred = true; return 0.0f; }
-        const float z2 = (float)h2 * tb.zw[i2];
+        const ZigLayer<float> l2 = tb.zig[i2];
+        if (!(a2 < l2.k)) { deferred = true; return 0.0f; }
+        const float z2 = (float)h2 * l2.w;
         return (z2 * sqrtf(kk) + kk) * inv_lambda;
     }
     if (draw) {
@@ -578,16 +587,17 @@ __device__ __forceinline__ float dornic_draw_fast(uint64_t seed, uint32_t site, 
         // control and the table loads issued together
         int it = 0;
         while (u < q && it < kFastInv) {
-            const float p1 = (p * m) * tb.rcp[it + 1];
+            const float4 r4 = *reinterpret_cast<const float4*>(tb.rcp + it + 1);
+            const float p1 = (p * m) * r4.x;
             const float q1 = q - p1;
             if (!(u < q1)) { it += 1; q = q1; break; }
-            const float p2 = (p1 * m) * tb.rcp[it + 2];
+            const float p2 = (p1 * m) * r4.y;
             const float q2 = q1 - p2;
             if (!(u < q2)) { it += 2; q = q2; break; }
-            const float p3 = (p2 * m) * tb.rcp[it + 3];
+            const float p3 = (p2 * m) * r4.z;
             const float q3 = q2 - p3;
             if (!(u < q3)) { it += 3; q = q3; break; }
-            p = (p3 * m) * tb.rcp[it + 4];
+            p = (p3 * m) * r4.w;
             q = q3 - p;
             it += 4;
         }
@@ -605,8 +615,9 @@ __device__ __forceinline__ float dornic_draw_fast(uint64_t seed, uint32_t site, 
     const int iz = zig_layer(wz);
     const int32_t hz = zig_value(wz);
     const uint32_t az = (uint32_t)(hz < 0 ? -hz : hz);
-    if (!(az < tb.zk[iz])) { deferred = true; return 0.0f; }
-    const float x = (float)hz * tb.zw[iz];
+    const ZigLayer<float> lz = tb.zig[iz];
+    if (!(az < lz.k)) { deferred = true; return 0.0f; }
+    const float x = (float)hz * lz.w;
     float v = 1.0f + c * x;
     if (!(v > 0.0f)) { deferred = true; return 0.0f; }
     const float mm = (v < 1.0f) ? v : 1.0f;
