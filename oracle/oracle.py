@@ -55,7 +55,7 @@ def lib():
         i64p = C.POINTER(C.c_int64)
         L.tmo_philox4x32_10.argtypes = [u32p, u32p, u32p]
         for nm, t in (("f64", C.c_double), ("f32", C.c_float)):
-            for fn in ("log", "exp", "log1p", "negexpm1"):
+            for fn in ("log", "exp", "log1p", "negexpm1", "inv_sqrt"):
                 f = getattr(L, f"tmo_{fn}_{nm}")
                 f.argtypes = [t]
                 f.restype = t

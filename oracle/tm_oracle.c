@@ -42,6 +42,7 @@ void tmo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t ou
 #define TC(x) ((double)(x))
 #define FMA fma
 #define SQRT sqrt
+#define INV_SQRT(x) (1.0 / sqrt(x))
 #define FABS fabs
 #define FLOOR floor
 #define RINT rint
@@ -58,6 +59,7 @@ void tmo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t ou
 #undef TC
 #undef FMA
 #undef SQRT
+#undef INV_SQRT
 #undef FABS
 #undef FLOOR
 #undef RINT
@@ -75,6 +77,9 @@ void tmo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t ou
 #define TC(x) ((float)(x))
 #define FMA fmaf
 #define SQRT sqrtf
+/* correctly rounded 1/sqrt(x) in float: the double quotient rounded once (checked
+ * exhaustively over [1, 4), which covers every normal float by scaling by 4) */
+#define INV_SQRT(x) ((float)(1.0 / sqrt((double)(x))))
 #define FABS fabsf
 #define FLOOR floorf
 #define RINT rintf

@@ -79,6 +79,8 @@ float    tmo_log_f32(float x);
 float    tmo_exp_f32(float x);
 float    tmo_log1p_f32(float x);
 float    tmo_negexpm1_f32(float m);
+double   tmo_inv_sqrt_f64(double x);    /* 1 / sqrt(x) */
+float    tmo_inv_sqrt_f32(float x);     /* correctly rounded 1 / sqrt(x) */
 
 /* Draw n variates; variate i uses the stream of (seed, site=i, step). */
 void tmo_sample_poisson_f64(double m, uint64_t seed, int64_t step, int sampler, int64_t n, double* out, uint32_t* status);

@@ -142,3 +142,35 @@ def test_dornic_draw_matches_libstdcxx(oracle, dtype):
                               dtype=dtype)
         assert st == 0
         assert stats.ks_2samp(x.astype(np.float64), ref).pvalue > 1e-3, (m, mu1)
+
+
+def _rsqrt_correct(x, r):
+    """r is the correctly rounded 1/sqrt(x): the interval of reals that round to r
+    contains 1/sqrt(x), i.e. lo^2 x <= 1 <= hi^2 x for its end points (exact)."""
+    from fractions import Fraction
+    import math
+    m, e = math.frexp(r)                       # r = m 2^e, m in [0.5, 1)
+    up = Fraction(2) ** (e - 24)               # ulp of r
+    down = up / 2 if m == 0.5 else up          # ulp below a power of two
+    fx, fr = Fraction(x), Fraction(r)
+    lo, hi = fr - down / 2, fr + up / 2
+    return lo * lo * fx <= 1 <= hi * hi * fx
+
+
+def test_inv_sqrt_f32_is_correctly_rounded(oracle):
+    """The Marsaglia-Tsang constant c = 1/sqrt(9d) in FP32 is the correctly rounded
+    1/sqrt, as __frsqrt_rn gives it in the kernels: the oracle rounds the double
+    quotient once.  An exhaustive exact check over [1, 4) (every normal float, by
+    scaling by 4) found no misrounding; this rechecks the inputs closest to a
+    rounding midpoint and 20000 random normal floats."""
+    hard = [float.fromhex(h) for h in ("0x1.7431c6p+1", "0x1.a4411ep+0", "0x1.fffffcp+1", "0x1.fbc3c2p+1",
+                                       "0x1.745472p+0", "0x1.13e07p+1", "0x1.14b90cp+0", "0x1.85da2cp+1",
+                                       "0x1.da646p+0", "0x1.b5d284p+0", "0x1.3ba2d4p+1", "0x1.fb7758p+1")]
+    rng = np.random.default_rng(5)
+    bits = rng.integers(0x00800000, 0x7f800000, 20000, dtype=np.uint32)
+    xs = [float(v) for v in bits.view(np.float32)] + [float(np.float32(h)) for h in hard]
+    bad = [x for x in xs if not _rsqrt_correct(x, float(oracle.scalar_fn("inv_sqrt", x, np.float32)))]
+    assert not bad, bad[:5]
+    # the two-rounding form 1.0f / sqrtf(x) differs on most of the hard inputs
+    two = [float(np.float32(1.0) / np.sqrt(np.float32(h))) for h in hard]
+    assert sum(not _rsqrt_correct(float(np.float32(h)), t) for h, t in zip(hard, two)) >= 1

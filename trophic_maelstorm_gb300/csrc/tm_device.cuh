@@ -51,6 +51,7 @@ template <typename T> struct Tr;
 template <> struct Tr<double> {
     static __device__ __forceinline__ double fma_(double a, double b, double c) { return fma(a, b, c); }
     static __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
+    static __device__ __forceinline__ double inv_sqrt(double x) { return 1.0 / sqrt(x); }
     static __device__ __forceinline__ double floor_(double x) { return floor(x); }
     static __device__ __forceinline__ double trunc_(double x) { return trunc(x); }
     static __device__ __forceinline__ double rint_(double x) { return rint(x); }
@@ -59,6 +60,8 @@ template <> struct Tr<double> {
 template <> struct Tr<float> {
     static __device__ __forceinline__ float fma_(float a, float b, float c) { return fmaf(a, b, c); }
     static __device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
+    // correctly rounded 1/sqrt(x) (one rounding, where 1.0f / sqrtf(x) rounds twice)
+    static __device__ __forceinline__ float inv_sqrt(float x) { return __frsqrt_rn(x); }
     static __device__ __forceinline__ float floor_(float x) { return floorf(x); }
     static __device__ __forceinline__ float trunc_(float x) { return truncf(x); }
     static __device__ __forceinline__ float rint_(float x) { return rintf(x); }
@@ -476,7 +479,7 @@ __device__ __forceinline__ T gamma_mt(Stream<T>& g, T k, const SmemTab<T>& tb)
     if (!(k > T(0))) return T(0);
     const T kk = (k < T(1)) ? k + T(1) : k;
     const T d = kk - T(1.0 / 3.0);
-    const T c = T(1) / Tr<T>::sqrt_(T(9) * d);
+    const T c = Tr<T>::inv_sqrt(T(9) * d);
     T res = kk;
     bool done = false;
     for (int it = 0; it < 64 && !done; ++it) {
@@ -611,7 +614,7 @@ __device__ __forceinline__ float dornic_draw_fast(uint64_t seed, uint32_t site, 
     const bool boost = k < 1.0f;            // Gamma(k) = Gamma(k+1) U^(1/k)
     const float kk = boost ? k + 1.0f : k;
     const float d = kk - (float)(1.0 / 3.0);
-    const float c = 1.0f / sqrtf(9.0f * d);
+    const float c = Tr<float>::inv_sqrt(9.0f * d);
     const int iz = zig_layer(wz);
     const int32_t hz = zig_value(wz);
     const uint32_t az = (uint32_t)(hz < 0 ? -hz : hz);
