@@ -5,6 +5,14 @@
 // columns, rows in order), a butterfly of shuffles combines the lanes, and
 // the per-task partials are summed per instance by one warp in task order.
 // No atomics, so a given state always gives the same bits.
+//
+// GB300's FP64 rate is a small fraction of its FP32 rate, so the per-site work
+// avoids FP64: active sites are counted with ballots, and an FP32 lane keeps
+// the sum of its column's values (at most 16) as an unevaluated pair hi + lo
+// by Knuth's TwoSum, which is exact up to the rounding of lo (relative 2^-48).
+// The lanes' pairs are combined the same way through the shuffle butterfly
+// (the values are non-negative, so nothing cancels), and lane 0 converts the
+// task's pair to FP64.
 #include "tm_device.cuh"
 #include "tm_kernels.cuh"
 
@@ -16,6 +24,42 @@ __device__ __forceinline__ double warp_sum(double v)
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
+
+// hi + lo += v with hi the rounded sum and its error carried in lo (TwoSum; the
+// kernels are built without contraction of multiply-adds, so every step rounds)
+__device__ __forceinline__ void two_sum_add(float& hi, float& lo, float v)
+{
+    const float s = hi + v;
+    const float bp = s - hi;
+    const float e = (hi - (s - bp)) + (v - bp);
+    hi = s;
+    lo = lo + e;
+}
+
+template <typename T>
+struct ColSum {
+    T s = T(0);
+    __device__ __forceinline__ void add(T v) { s += v; }
+    __device__ __forceinline__ double warp_total() const { return warp_sum((double)s); }
+};
+template <>
+struct ColSum<float> {
+    float hi = 0.0f, lo = 0.0f;
+    __device__ __forceinline__ void add(float v) { two_sum_add(hi, lo, v); }
+    // sum over the warp, valid in lane 0
+    __device__ __forceinline__ double warp_total() const
+    {
+        float h = hi, l = lo;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float ho = __shfl_down_sync(0xffffffffu, h, o);
+            const float lo2 = __shfl_down_sync(0xffffffffu, l, o);
+            two_sum_add(h, l, ho);
+            l = l + lo2;
+        }
+        return (double)h + (double)l;
+    }
+};
 
 // partial[t*4 + f]: f = 0..nf-1 field sums, 3 = sites with field 0 > 0
 template <typename T>
@@ -30,29 +74,32 @@ __global__ void __launch_bounds__(256) measure_kernel(const T* state, const Inst
         const int k = tk.x;
         const int L = it.L[k];
         const int x = tk.y + lane;
-        double s0 = 0.0, s1 = 0.0, s2 = 0.0, ac = 0.0;
-        if (x < L && (it.alive == nullptr || it.alive[k] != 0)) {
+        ColSum<T> c0, c1, c2;
+        int ac = 0;
+        const bool on = it.alive == nullptr || it.alive[k] != 0;   // warp-uniform
+        if (on) {
             const T* base = state + it.off[k];
             const long long fs = it.fstride[k];
+            const bool in = x < L;
             for (int r = 0; r < tk.w; ++r) {
                 const long long i = (long long)(tk.z + r) * L + x;
-                const T v = base[i];
-                s0 += (double)v;
-                if (v > T(0)) ac += 1.0;
-                if (nf == 3) {
-                    s1 += (double)base[i + fs];
-                    s2 += (double)base[i + 2 * fs];
+                const T v = in ? base[i] : T(0);
+                c0.add(v);
+                ac += __popc(__ballot_sync(0xffffffffu, v > T(0)));
+                if (nf == 3 && in) {
+                    c1.add(base[i + fs]);
+                    c2.add(base[i + 2 * fs]);
                 }
             }
         }
-        s0 = warp_sum(s0);
-        ac = warp_sum(ac);
-        if (nf == 3) { s1 = warp_sum(s1); s2 = warp_sum(s2); }
+        const double s0 = c0.warp_total();
+        double s1 = 0.0, s2 = 0.0;
+        if (nf == 3) { s1 = c1.warp_total(); s2 = c2.warp_total(); }
         if (lane == 0) {
             partial[4LL * t + 0] = s0;
             partial[4LL * t + 1] = s1;
             partial[4LL * t + 2] = s2;
-            partial[4LL * t + 3] = ac;
+            partial[4LL * t + 3] = (double)ac;
         }
     }
 }
