@@ -129,7 +129,8 @@ def test_launch_shape_and_path_invariance(tmg, ctx, precision):
     dtype = np.float64 if precision == 0 else np.float32
     init = [f.astype(dtype) for f in _init_fields(Ls, 3)]
     res = []
-    for rows, ctas, chunks in ((8, 4, [70]), (4, 2, [70]), (16, 8, [70]), (16, 1, [1] * 70)):
+    for rows, ctas, chunks in ((8, 4, [70]), (4, 2, [70]), (16, 8, [70]), (16, 1, [1] * 70), (1, 4, [70]),
+                               (2, 3, [70])):
         b = tmg.Batch(ctx, model, inst, precision)
         b.set_launch(rows, ctas)
         b.upload(init)
@@ -139,6 +140,17 @@ def test_launch_shape_and_path_invariance(tmg, ctx, precision):
         b.close()
     for r in res[1:]:
         assert np.array_equal(r, res[0])
+
+
+def test_small_batch_gets_short_tasks(tmg, ctx):
+    """A batch with too few 8-row tasks to fill the GPU starts with fewer rows per task
+    (one 128^2 lattice: 64 tasks of 8 rows); a large batch keeps 8."""
+    small = tmg.Batch(ctx, tmg.dp_model(), tmg.instances([128], [1], 0.72), 0)
+    assert small.get_launch()[0] < 8
+    small.close()
+    big = tmg.Batch(ctx, tmg.dp_model(), tmg.instances([1024] * 4, [1, 2, 3, 4], 0.72), 1)
+    assert big.get_launch()[0] == 8
+    big.close()
 
 
 @pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32"])
