@@ -53,3 +53,27 @@ def test_features_scale_the_window_to_unit_range():
     from trophic_maelstorm_gb300 import surrogate as sg
     f = sg.features([0.50, 0.56], [64, 1024], [1.0, 1000.0])
     np.testing.assert_allclose(f, [[-1, -1, -1], [1, 1, 1]], atol=1e-6)
+
+
+def test_judge_uses_common_random_numbers(monkeypatch):
+    """Every value of a is judged with the same replicate keys (initial fields and Philox
+    streams), so two judges with the same seed see the same delta_eff(a) and the
+    values differ by the control parameter only; cached values are not re-run."""
+    from trophic_maelstorm_gb300 import surrogate as sg
+    calls = []
+
+    def fake_run(ctx, a_values, L, n_rep, t_max, point_seeds=None, **kw):
+        calls.append((list(a_values), list(point_seeds)))
+        t = np.array([1.0, 100.0, 1000.0])
+        rho = np.array([[1.0, 0.1, 0.1 * 10 ** (-(0.45 + (0.53 - a)))] for a in a_values])
+        return sg.Ensembles(np.asarray(a_values), np.full(len(a_values), L), t, rho, np.ones_like(rho), n_rep,
+                            0.0, 0.0)
+
+    monkeypatch.setattr(sg, "run_ensembles", fake_run)
+    j = sg.Judge(None, 64, 4, 1000.0, 100.0, seed=7)
+    d1 = j.delta([0.52, 0.54])
+    d2 = j.delta([0.54, 0.53])
+    assert len(calls) == 2 and calls[1][0] == [0.53]            # 0.54 came from the cache
+    assert all(s == 7 for _, seeds in calls for s in seeds)      # one key set for every a
+    assert d1[1] == d2[0] and j.runs == 3 * 4
+    assert d1[0] > d2[1] > d1[1]                                 # decreasing in a
