@@ -69,7 +69,46 @@ def test_replicate_rows_statistics():
 
 
 def test_invalid_arguments_are_rejected_without_gpu(tmlib):
+    """Every entry point answers a NULL handle, a NULL buffer or an impossible size with
+    TM_ERR_INVALID before it touches the device (the reference exits instead)."""
     L = tmlib.lib()
-    assert L.tm_create(None, 0) == tmlib.TM_ERR_INVALID
-    assert L.tm_destroy(None) == tmlib.TM_ERR_INVALID
-    assert L.tm_batch_step(None) == -1
+    bad = tmlib.TM_ERR_INVALID
+    assert L.tm_create(None, 0) == bad
+    assert L.tm_destroy(None) == bad
+    assert L.tm_batch_step(None) == bad
+    calls = {
+        "tm_batch_create_dp": (None, None, None, 0, 1, None),
+        "tm_batch_create_rietkerk": (None, None, None, 0, 1, None),
+        "tm_batch_destroy": (None,),
+        "tm_batch_total_elems": (None,),
+        "tm_batch_instance_offset": (None, 0),
+        "tm_batch_field_stride": (None, 0),
+        "tm_batch_upload": (None, None, 0),
+        "tm_batch_download": (None, None),
+        "tm_batch_upload_device": (None, None, 0),
+        "tm_batch_download_device": (None, None),
+        "tm_batch_snapshot": (None, 0, None),
+        "tm_batch_advance": (None, 1, None, 0, None, None),
+        "tm_batch_enqueue_steps": (None, 1),
+        "tm_batch_set_launch": (None, 8, 4),
+        "tm_batch_get_launch": (None, None, None),
+        "tm_batch_autotune": (None, 2),
+        "tm_batch_set_site_coeff": (None, None),
+        "tm_batch_box_means": (None, 0, 0, 4, None),
+        "tm_batch_power_spectrum": (None, 0, 0, 0.5, None, None, 0, None),
+        "tm_run_dp": (None, None, None, 1, 1, None, 1, None, 0, None, None, None),
+        "tm_run_rietkerk": (None, None, None, 1, 1, None, 1, None, 0, None, None, None),
+        "tm_observe_noalloc": (None, 1, None, None, 1, None, None),
+        "tm_power_spectrum_device": (None, 1, 0, 0.5, None, None, None, 10, None),
+        "tm_fke_advdiff_device": (None, None, None, None, 1, 0, 1.0, 1e-10, None, 1, None, 1, None, None),
+        "tm_mlp_create": (None, None, None),
+        "tm_mlp_destroy": (None,),
+        "tm_mlp_set_params": (None, None),
+        "tm_mlp_get_params": (None, None),
+        "tm_mlp_set_data": (None, None, None, None, 0),
+        "tm_mlp_loss_grad": (None, 1.0, None, None),
+        "tm_mlp_train": (None, 1, 1e-3, 0.9, 0.999, 1e-8, 1.0, None),
+        "tm_mlp_predict": (None, None, 0, None),
+    }
+    for name, args in calls.items():
+        assert getattr(L, name)(*args) == bad, name
