@@ -2,12 +2,14 @@
 //
 // One warp owns a strip of 32 columns x R rows (R <= 16) of one instance
 // ("task") and walks down it with a three-row register window (north,
-// centre, south); east/west neighbours come from warp shuffles, the two
-// strip-edge columns from global memory.  Each lattice value is read from HBM
-// once per step and written once (8 B per site-update in FP32).  Sites that
-// need a random draw are compacted into a per-warp queue in shared memory so
-// that every lane of the sampler loop works on a live site: absorbing sites
-// never occupy a sampler lane.  Per site it fuses:
+// centre, south; the next row is read one row ahead); east/west neighbours
+// come from warp shuffles, the two strip-edge columns from one read per task.
+// Each lattice value is read from HBM once per step and written once (8 B per
+// site-update in FP32).  Sites that need a random draw are compacted into a
+// per-warp queue in shared memory so that every lane of the sampler loop works
+// on a live site: absorbing sites never occupy a sampler lane.  FP32 draws take
+// a straight-line path first; the few sites it defers are carried from task to
+// task and drawn by the general sampler 32 at a time.  Per site it fuses:
 //   alpha_i  = (D/dx^2) * sum of the 4 neighbours       stochasticSPDP.cpp:1037-1038
 //   skip     if alpha_i == 0 and rho_i == 0             :1049-1052
 //   rho*     = Gamma(2 alpha_i/sigma^2 + Poisson(lambda e^{beta dt} rho_i)) / lambda   :1053-1059
