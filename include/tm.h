@@ -51,6 +51,10 @@ extern "C" {
 #define TM_STATUS_NAN          0x1u  /* NaN or Inf produced               */
 #define TM_STATUS_NEGATIVE     0x2u  /* negative density produced         */
 #define TM_STATUS_SAMPLER_CAP  0x4u  /* a rejection loop hit its cap      */
+#define TM_STATUS_WAIT_TIMEOUT 0x8u  /* a bounded wait for a tile copy ran
+                                        out: the instance's fields are
+                                        invalid from that step on, and the
+                                        call returns TM_ERR_TIMEOUT        */
 
 /* precision of the field state; reductions are FP64 in both */
 #define TM_FP64 0
@@ -160,8 +164,13 @@ int tm_batch_snapshot(tm_batch* b, int k, void* host_out);
  * instance measured with no active site is extinct: it stays zero and its
  * later measurements are 0 (the early exit of stochasticSPDP.cpp:1021-1022).
  * status (optional, n_inst entries) receives the OR of TM_STATUS_* bits since
- * creation or the last upload.  obs may be NULL when n_meas == 0.
- * The call returns after the work is queued and complete (it synchronises). */
+ * creation or the last upload, including those of the uploaded state itself
+ * (tm_batch_upload marks a NaN/Inf with TM_STATUS_NAN and a negative value with
+ * TM_STATUS_NEGATIVE, as the reference's per-step checks would on its next
+ * step, multiSPDP.cpp:2949-2955, 3237-3255).  obs may be NULL when n_meas == 0.
+ * Returns TM_ERR_TIMEOUT (after filling obs and status) when an instance got
+ * TM_STATUS_WAIT_TIMEOUT.  The call returns after the work is queued and
+ * complete (it synchronises). */
 int tm_batch_advance(tm_batch* b, int64_t n_steps, const int64_t* meas_steps, int n_meas,
                      double* obs, uint32_t* status);
 /* Same, without synchronising and without measurements: queues n_steps steps on
@@ -219,7 +228,12 @@ int tm_run_rietkerk(tm_ctx* ctx, const tm_rietkerk_model* model, const tm_instan
  * plus 24 bytes per 32-column strip (sum over instances of ceil(L/32)).
  * The first call on a device looks up the array's device address (once per
  * device, with that device current); make that first call before any stream
- * capture.  All calls share the one array and leave their contents in it;
+ * capture.  The address is kept for the life of the process, so the entry
+ * point must not be called on a device after cudaDeviceReset of that device.
+ * L and offsets are copied to the scratch by an asynchronous copy on `stream`:
+ * keep them unchanged until the stream has passed the call (page-locked host
+ * arrays are read by that copy after the call returns).
+ * All calls share the one array and leave their contents in it;
  * every value a call reads it has written itself, so nothing needs clearing,
  * but two calls that overlap on the GPU (other streams, other host threads)
  * race on the array: order them on one stream or synchronise between them.
@@ -288,7 +302,8 @@ int tm_fke_advdiff_device(const void* dev_rho, const void* dev_gamma, const void
  * bit-reproducible.  The optimiser is full-batch Adam on the FP32 masters,
  * with bias corrections 1/(1 - beta^t) computed on the host in double.
  * tm_mlp_train returns TM_ERR_TIMEOUT if a bounded wait for a tensor-core
- * operation ran out (the context stays usable). */
+ * operation ran out (the context stays usable; the parameters keep their value
+ * from before the step whose wait ran out). */
 #define TM_MLP_NPARAMS 33794
 typedef struct tm_mlp tm_mlp;
 int tm_mlp_create(tm_ctx* ctx, const float* params, tm_mlp** out);
@@ -305,6 +320,30 @@ int tm_mlp_train(tm_mlp* m, int steps, float lr, float beta1, float beta2, float
                  double* loss_hist);
 /* y (n x 2) for features x (n x 3) */
 int tm_mlp_predict(tm_mlp* m, const float* x, int n, float* y);
+
+/* -- failure probes (tests only) -----------------------------------------
+ * Each flag makes one failure path of the library run on purpose, in a form
+ * that faults nothing, so a test can check what the caller sees:
+ *   TM_PROBE_SAMPLER_CAP1  every rejection loop of the samplers stops after one
+ *                          attempt: sites whose first attempt is rejected get
+ *                          TM_STATUS_SAMPLER_CAP (and the loop's fallback value);
+ *                          DP batches with the Euler-exact remainder and the
+ *                          exact sampler only (others: TM_ERR_INVALID)
+ *   TM_PROBE_TILE_WAIT     the Rietkerk RK4 tiles issue no copy and wait on a
+ *                          barrier nothing arrives at: the bounded wait runs out
+ *                          with nothing in flight, the instances get
+ *                          TM_STATUS_WAIT_TIMEOUT and tm_batch_advance returns
+ *                          TM_ERR_TIMEOUT
+ *   TM_PROBE_MLP_WAIT      the network kernel issues no MMA and waits for a commit
+ *                          that never comes: tm_mlp_* return TM_ERR_TIMEOUT and
+ *                          leave the parameters unchanged
+ * The flags apply to batches created, and network calls made, after this call
+ * on this context (a batch's step graphs keep its launch arguments); 0 clears
+ * them.  The context stays usable in every case. */
+#define TM_PROBE_SAMPLER_CAP1 0x1u
+#define TM_PROBE_TILE_WAIT    0x2u
+#define TM_PROBE_MLP_WAIT     0x4u
+int tm_set_test_probe(tm_ctx* ctx, uint32_t flags);
 
 /* Packed-layout geometry without a batch (for callers that pack host buffers
  * before creating one): offsets[k] and the total, for nf fields per instance. */

@@ -79,6 +79,7 @@ def lib():
                                                        C.c_int, dp, dp, ptr, u32p]
         L.tmo_fke_advdiff_f64.argtypes = [C.c_int, dp, dp, dp, dp, C.c_double, C.c_double, dp, C.c_int, dp, C.c_int,
                                           dp]
+        L.tmo_set_sampler_cap.argtypes = [C.c_int]
         L.tmo_dornic_consts_compute.argtypes = [C.c_double] * 5 + [C.POINTER(DornicConsts)]
         L.tmo_dp_batch_run_f32.argtypes = [C.POINTER(DPParams), C.POINTER(C.c_int), C.POINTER(C.c_uint64),
                                            C.POINTER(fp), C.c_int, C.c_int64, C.c_int]
@@ -100,6 +101,11 @@ def _ptr(a):
 
 def _sfx(dtype):
     return "f64" if np.dtype(dtype) == np.float64 else "f32"
+
+
+def set_sampler_cap(cap=64):
+    """Attempts of every rejection loop (64 by default; 1 matches TM_PROBE_SAMPLER_CAP1)."""
+    lib().tmo_set_sampler_cap(int(cap))
 
 
 def philox(ctr, key):

@@ -14,6 +14,12 @@
 
 #include "tm_zig_table.inc"
 
+/* attempts of every rejection loop of the samplers before TMO_STATUS_SAMPLER_CAP
+ * (the library's kSamplerCap; tests lower it to 1 to make the cap path run, as
+ * the library's TM_PROBE_SAMPLER_CAP1 does) */
+static int tmo_cap = 64;
+void tmo_set_sampler_cap(int cap) { tmo_cap = cap < 1 ? 1 : cap; }
+
 /* Philox4x32-10: J. K. Salmon, M. A. Moraes, R. O. Dror, D. E. Shaw,
  * "Parallel random numbers: as easy as 1, 2, 3", SC'11.  Ten rounds of
  * (c0,c1,c2,c3) -> (hi(M1 c2)^c1^k0, lo(M1 c2), hi(M0 c0)^c3^k1, lo(M0 c0))

@@ -69,6 +69,10 @@ typedef struct {
     int sampler;
 } tmo_rk_params;
 
+/* attempts of every rejection loop of the samplers (default 64, the library's;
+ * 1 reproduces the library under TM_PROBE_SAMPLER_CAP1) */
+void     tmo_set_sampler_cap(int cap);
+
 /* -- primitives ---------------------------------------------------------- */
 void     tmo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 double   tmo_log_f64(double x);

@@ -1,8 +1,9 @@
 """Generate the golden fixtures in this folder from the reference's own code.
 
 Needs the reference checkout and its harness libraries, built by
-`make -C oracle ref` (REF_ROOT defaults to the reference mount of the
-development container).  The fixtures are committed; tests only read them.
+`make -C oracle ref REF_ROOT=<reference checkout>` (__graft_entry__.build()
+runs it where the checkout exists).  The fixtures are committed; tests only
+read them.
 
     python tests/golden/gen_golden.py
 

@@ -13,7 +13,8 @@ LIB_PATH = os.path.join(PKG, "lib", "libtm.so")
 
 TM_OK, TM_ERR_INVALID, TM_ERR_CUDA, TM_ERR_NOMEM, TM_ERR_STATE, TM_ERR_TIMEOUT = 0, -1, -2, -3, -4, -5
 TM_MLP_NPARAMS = 33794
-TM_STATUS_NAN, TM_STATUS_NEGATIVE, TM_STATUS_SAMPLER_CAP = 0x1, 0x2, 0x4
+TM_STATUS_NAN, TM_STATUS_NEGATIVE, TM_STATUS_SAMPLER_CAP, TM_STATUS_WAIT_TIMEOUT = 0x1, 0x2, 0x4, 0x8
+TM_PROBE_SAMPLER_CAP1, TM_PROBE_TILE_WAIT, TM_PROBE_MLP_WAIT = 0x1, 0x2, 0x4
 TM_FP64, TM_FP32 = 0, 1
 TM_REM_EULER_EXACT, TM_REM_RK4 = 0, 1
 TM_SAMPLER_EXACT, TM_SAMPLER_REF_GAUSS100, TM_SAMPLER_OFF = 0, 1, 2
@@ -30,7 +31,7 @@ EXPORTS = (
     "tm_layout", "tm_observe_noalloc", "tm_power_spectrum_device", "tm_batch_power_spectrum",
     "tm_batch_set_site_coeff", "tm_batch_box_means", "tm_fke_advdiff_device",
     "tm_mlp_create", "tm_mlp_destroy", "tm_mlp_set_params", "tm_mlp_get_params", "tm_mlp_set_data",
-    "tm_mlp_loss_grad", "tm_mlp_train", "tm_mlp_predict",
+    "tm_mlp_loss_grad", "tm_mlp_train", "tm_mlp_predict", "tm_set_test_probe",
 )
 
 
@@ -120,6 +121,7 @@ def lib():
             "tm_mlp_loss_grad": ([vp, C.c_float, dp, fp], C.c_int),
             "tm_mlp_train": ([vp, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, dp], C.c_int),
             "tm_mlp_predict": ([vp, fp, C.c_int, fp], C.c_int),
+            "tm_set_test_probe": ([vp, C.c_uint32], C.c_int),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)

@@ -95,6 +95,10 @@ class Context:
     def sync(self):
         T.check(T.lib().tm_sync(self._h), "tm_sync")
 
+    def set_test_probe(self, flags: int = 0):
+        """Make a failure path run on purpose (TM_PROBE_*; tests only); 0 clears."""
+        T.check(T.lib().tm_set_test_probe(self._h, int(flags)), "tm_set_test_probe")
+
     def close(self):
         if self._h:
             T.lib().tm_destroy(self._h)

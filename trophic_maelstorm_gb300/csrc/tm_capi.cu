@@ -83,6 +83,7 @@ struct tm_batch {
     unsigned* d_status = nullptr;
     bool ramped = false;
 
+    unsigned probe = 0;         // TM_PROBE_* flags of the context when the batch was created
     int rows_per_task = 8;
     int ctas_per_sm = 4;
     int4* d_tasks = nullptr;
@@ -185,6 +186,7 @@ DornicArgs<T> dornic_args(const tm_batch* b, const T* in, T* out, const long lon
     DornicArgs<T> a{};
     a.in = in; a.out = out; a.it = b->tables(); a.tasks = b->d_tasks; a.n_tasks = b->n_tasks;
     a.step_base = step_base; a.step_off = step_off; a.rows_cap = b->rows_per_task;
+    a.cap1 = (b->probe & TM_PROBE_SAMPLER_CAP1) ? 1 : 0;
     a.site_b = (b->model == 0) ? (const T*)b->site_b : nullptr;
     if (b->model == 0) {
         const tm_dp_model& m = b->dpm;
@@ -220,6 +222,8 @@ RK4Args<T> rk4_args(const tm_batch* b, const T* in, const T* pstar, T* out)
     a.DPx = (T)(m.DP / dx2); a.DWx = (T)(m.DW / dx2); a.DOx = (T)(m.DO / dx2);
     a.dt2 = (T)(m.dt / 2.0); a.dt6 = (T)(m.dt / 6.0); a.dt = (T)m.dt;
     a.clo = (T)m.clamp_lo; a.ceps = (T)m.clamp_eps;
+    a.probe_no_copy = (b->probe & TM_PROBE_TILE_WAIT) ? 1 : 0;
+    a.wait_limit = a.probe_no_copy ? (1 << 14) : (1 << 22);
     return a;
 }
 
@@ -392,6 +396,7 @@ int batch_common_init(tm_batch* b, const tm_instance* inst, int n)
     TM_CUDA(cudaMemcpy(b->d_alive, ones.data(), n * sizeof(int), cudaMemcpyHostToDevice));
     TM_CUDA(cudaMemset(b->d_status, 0, n * sizeof(unsigned)));
     TM_CUDA(cudaMemset(b->d_step, 0, sizeof(long long)));
+    b->probe = b->ctx->probe;
     b->rows_per_task = default_rows(b);
     return build_tasks(b);
 }
@@ -473,6 +478,13 @@ int tm_destroy(tm_ctx* c)
 
 void* tm_stream(tm_ctx* c) { return c ? (void*)c->stream : nullptr; }
 
+int tm_set_test_probe(tm_ctx* c, uint32_t flags)
+{
+    if (!c || (flags & ~(TM_PROBE_SAMPLER_CAP1 | TM_PROBE_TILE_WAIT | TM_PROBE_MLP_WAIT))) return TM_ERR_INVALID;
+    c->probe = flags;
+    return TM_OK;
+}
+
 int tm_sync(tm_ctx* c)
 {
     if (!c) return TM_ERR_INVALID;
@@ -513,6 +525,10 @@ int tm_batch_create_dp(tm_ctx* c, const tm_dp_model* m, const tm_instance* inst,
         if (m->sampler < 0 || m->sampler > 2) return TM_ERR_INVALID;
         if (m->sampler != TM_SAMPLER_OFF && !(m->sigma > 0)) return TM_ERR_INVALID;
     }
+    // the sampler-cap probe exists for the Euler-exact, exact-sampler Dornic step only
+    if ((c->probe & TM_PROBE_SAMPLER_CAP1) &&
+        (m->deterministic || m->remainder != TM_REM_EULER_EXACT || m->sampler != TM_SAMPLER_EXACT))
+        return TM_ERR_INVALID;
     TM_CUDA(cudaSetDevice(c->device));
     tm_batch* b = new (std::nothrow) tm_batch;
     if (!b) return TM_ERR_NOMEM;
@@ -548,6 +564,7 @@ int tm_batch_create_rietkerk(tm_ctx* c, const tm_rietkerk_model* m, const tm_ins
     if (!(m->dt > 0) || !(m->dx > 0)) return TM_ERR_INVALID;
     if (!m->deterministic && (m->sampler < 0 || m->sampler > 2)) return TM_ERR_INVALID;
     if (!m->deterministic && m->sampler != TM_SAMPLER_OFF && !(m->sigma > 0)) return TM_ERR_INVALID;
+    if (c->probe & TM_PROBE_SAMPLER_CAP1) return TM_ERR_INVALID;
     TM_CUDA(cudaSetDevice(c->device));
     tm_batch* b = new (std::nothrow) tm_batch;
     if (!b) return TM_ERR_NOMEM;
@@ -585,20 +602,27 @@ int tm_batch_num_fields(const tm_batch* b) { return b ? b->nf : -1; }
 int tm_batch_obs_width(const tm_batch* b) { return b ? (b->model == 0 ? 2 : 4) : -1; }
 int64_t tm_batch_step(const tm_batch* b) { return b ? b->step : -1; }
 
+// After an upload: step counter, extinction flags, and the status bits of the
+// uploaded state itself (NaN/Inf, negative values).
 static int reset_after_upload(tm_batch* b, int64_t step)
 {
-    if (step < 0) return TM_ERR_INVALID;
     b->step = step;
+    cudaStream_t s = b->ctx->stream;
     std::vector<int> ones(b->n_inst, 1);
-    TM_CUDA(cudaMemcpyAsync(b->d_alive, ones.data(), b->n_inst * sizeof(int), cudaMemcpyHostToDevice, b->ctx->stream));
-    TM_CUDA(cudaMemsetAsync(b->d_status, 0, b->n_inst * sizeof(unsigned), b->ctx->stream));
-    TM_CUDA(cudaStreamSynchronize(b->ctx->stream));
+    TM_CUDA(cudaMemcpyAsync(b->d_alive, ones.data(), b->n_inst * sizeof(int), cudaMemcpyHostToDevice, s));
+    TM_CUDA(cudaMemsetAsync(b->d_status, 0, b->n_inst * sizeof(unsigned), s));
+    InstTables it = b->tables();
+    const int grid = warp_grid(b, b->n_tasks);
+    TM_CUDA(b->precision == TM_FP64
+                ? launch_validate<double>((const double*)b->buf[b->cur], it, b->d_tasks, b->n_tasks, b->nf, grid, s)
+                : launch_validate<float>((const float*)b->buf[b->cur], it, b->d_tasks, b->n_tasks, b->nf, grid, s));
+    TM_CUDA(cudaStreamSynchronize(s));
     return TM_OK;
 }
 
 int tm_batch_upload(tm_batch* b, const void* host, int64_t step)
 {
-    if (!b || !host) return TM_ERR_INVALID;
+    if (!b || !host || step < 0) return TM_ERR_INVALID;
     TM_CUDA(cudaSetDevice(b->ctx->device));
     TM_CUDA(cudaMemcpyAsync(b->buf[b->cur], host, (size_t)b->total * b->esize, cudaMemcpyHostToDevice, b->ctx->stream));
     return reset_after_upload(b, step);
@@ -606,7 +630,7 @@ int tm_batch_upload(tm_batch* b, const void* host, int64_t step)
 
 int tm_batch_upload_device(tm_batch* b, const void* dev, int64_t step)
 {
-    if (!b || !dev) return TM_ERR_INVALID;
+    if (!b || !dev || step < 0) return TM_ERR_INVALID;
     TM_CUDA(cudaSetDevice(b->ctx->device));
     TM_CUDA(cudaMemcpyAsync(b->buf[b->cur], dev, (size_t)b->total * b->esize, cudaMemcpyDeviceToDevice,
                             b->ctx->stream));
@@ -698,10 +722,16 @@ int tm_batch_advance(tm_batch* b, int64_t n_steps, const int64_t* meas, int n_me
     if (n_meas > 0)
         TM_CUDA(cudaMemcpyAsync(obs, b->d_obs, (size_t)n_meas * b->n_inst * W * sizeof(double),
                                 cudaMemcpyDeviceToHost, b->ctx->stream));
-    if (status)
-        TM_CUDA(cudaMemcpyAsync(status, b->d_status, b->n_inst * sizeof(unsigned), cudaMemcpyDeviceToHost,
-                                b->ctx->stream));
+    std::vector<uint32_t> st_local;
+    uint32_t* st = status;
+    if (!st) {
+        st_local.resize(b->n_inst);
+        st = st_local.data();
+    }
+    TM_CUDA(cudaMemcpyAsync(st, b->d_status, b->n_inst * sizeof(unsigned), cudaMemcpyDeviceToHost, b->ctx->stream));
     TM_CUDA(cudaStreamSynchronize(b->ctx->stream));
+    for (int k = 0; k < b->n_inst; ++k)
+        if (st[k] & TM_STATUS_WAIT_TIMEOUT) return TM_ERR_TIMEOUT;
     return TM_OK;
 }
 

@@ -26,6 +26,7 @@
 #define TM_STATUS_NAN_BIT 0x1u
 #define TM_STATUS_NEG_BIT 0x2u
 #define TM_STATUS_CAP_BIT 0x4u
+#define TM_STATUS_WAIT_BIT 0x8u
 
 namespace tmg {
 
@@ -312,7 +313,7 @@ struct Stream {
     }
     // uniform on (0,1)
     __device__ __forceinline__ T open();
-    template <class Tab>
+    template <int CAP, class Tab>
     __device__ __forceinline__ T normal(const Tab& tb);
 };
 
@@ -344,6 +345,10 @@ static_assert(kZigN == (1 << kZigBits), "ziggurat layer count");
 // sits on a 16-byte boundary: the straight-line inversion reads rcp[it+1..it+4]
 // with one vector load.
 constexpr int kRcpTable = 201;
+// Attempts of every rejection loop before TM_STATUS_CAP_BIT: the samplers take
+// it as a template argument CAP, kSamplerCap everywhere but in the one kernel
+// instantiation a test uses to make the cap path run (CAP = 1).
+constexpr int kSamplerCap = 64;
 template <typename T>
 struct ZigLayer {
     uint32_t k;
@@ -368,10 +373,10 @@ static_assert(sizeof(ZigLayer<float>) == 8, "one 8-byte load per layer");
 // from the low kZigBits bits, signed value from the rest), wedge test or
 // Marsaglia's tail method when the fast test fails.
 template <typename T>
-template <class Tab>
+template <int CAP, class Tab>
 __device__ __forceinline__ T Stream<T>::normal(const Tab& tb)
 {
-    for (int it = 0; it < 64; ++it) {
+    for (int it = 0; it < CAP; ++it) {
         const uint32_t w = u32();
         const int iz = zig_layer(w);
         const int32_t hz = zig_value(w);
@@ -380,7 +385,7 @@ __device__ __forceinline__ T Stream<T>::normal(const Tab& tb)
         const T x = (T)hz * zl.w;
         if (az < zl.k) return x;
         if (iz == 0) {
-            for (int jt = 0; jt < 64; ++jt) {
+            for (int jt = 0; jt < CAP; ++jt) {
                 const T xt = -tm_log_pos(open()) * T(1.0 / kZigR);
                 const T yt = -tm_log_pos(open());
                 if (yt + yt >= xt * xt) {
@@ -420,7 +425,7 @@ __device__ __forceinline__ double logfact_small(int k)
 }
 
 // ---------------------------------------------------------------- samplers
-template <typename T>
+template <int CAP, typename T>
 __device__ __forceinline__ T poisson_exact(Stream<T>& g, T m, const SmemTab<T>& tb)
 {
     if (!(m > T(0))) return T(0);
@@ -448,7 +453,7 @@ __device__ __forceinline__ T poisson_exact(Stream<T>& g, T m, const SmemTab<T>& 
     const T invalpha = T(1.1239) + T(1.1328) / (b - T(3.4));
     const T vr = T(0.9277) - T(3.6224) / (b - T(2));
     const T loginvalpha = tm_log_pos(invalpha);
-    for (int it = 0; it < 64; ++it) {
+    for (int it = 0; it < CAP; ++it) {
         const T U = g.open() - T(0.5);
         const T V = g.open();
         const T us = T(0.5) - Tr<T>::fabs_(U);
@@ -473,7 +478,7 @@ __device__ __forceinline__ T poisson_exact(Stream<T>& g, T m, const SmemTab<T>& 
     return Tr<T>::floor_(m);
 }
 
-template <typename T>
+template <int CAP, typename T>
 __device__ __forceinline__ T gamma_mt(Stream<T>& g, T k, const SmemTab<T>& tb)
 {
     if (!(k > T(0))) return T(0);
@@ -482,11 +487,11 @@ __device__ __forceinline__ T gamma_mt(Stream<T>& g, T k, const SmemTab<T>& tb)
     const T c = Tr<T>::inv_sqrt(T(9) * d);
     T res = kk;
     bool done = false;
-    for (int it = 0; it < 64 && !done; ++it) {
+    for (int it = 0; it < CAP && !done; ++it) {
         T x = T(0), v = T(0);
         bool ok = false;
-        for (int jt = 0; jt < 64; ++jt) {
-            x = g.normal(tb);
+        for (int jt = 0; jt < CAP; ++jt) {
+            x = g.template normal<CAP>(tb);
             v = T(1) + c * x;
             if (v > T(0)) { ok = true; break; }
         }
@@ -507,35 +512,35 @@ __device__ __forceinline__ T gamma_mt(Stream<T>& g, T k, const SmemTab<T>& tb)
 }
 
 // sampler: 0 exact, 1 Gaussian above 100 (multiSPDP.cpp:2915-2943)
-template <typename T>
+template <int CAP, typename T>
 __device__ __forceinline__ T poisson_draw(Stream<T>& g, T m, int sampler, const SmemTab<T>& tb)
 {
     if (!(m > T(0))) return T(0);
     if (sampler == 1 && m > T(100)) {
-        const T z = g.normal(tb);
+        const T z = g.template normal<CAP>(tb);
         return Tr<T>::trunc_(z * Tr<T>::sqrt_(m) + m);
     }
-    return poisson_exact(g, m, tb);
+    return poisson_exact<CAP>(g, m, tb);
 }
 
-template <typename T>
+template <int CAP, typename T>
 __device__ __forceinline__ T gamma_draw(Stream<T>& g, T k, int sampler, const SmemTab<T>& tb)
 {
     if (sampler == 1 && k > T(100)) {
-        const T z = g.normal(tb);
+        const T z = g.template normal<CAP>(tb);
         return z * Tr<T>::sqrt_(k) + k;
     }
-    return gamma_mt(g, k, tb);
+    return gamma_mt<CAP>(g, k, tb);
 }
 
 // rho* = Gamma(mu1 + Poisson(m)) / lambda  (stochasticSPDP.cpp:1053-1059)
-template <typename T>
+template <int CAP, typename T>
 __device__ __forceinline__ T dornic_draw(Stream<T>& g, T m, T mu1, T inv_lambda, int sampler,
                                         const SmemTab<T>& tb)
 {
-    const T n = poisson_draw(g, m, sampler, tb);
+    const T n = poisson_draw<CAP>(g, m, sampler, tb);
     const T k = mu1 + n;
-    const T gv = gamma_draw(g, k, sampler, tb);
+    const T gv = gamma_draw<CAP>(g, k, sampler, tb);
     return gv * inv_lambda;
 }
 

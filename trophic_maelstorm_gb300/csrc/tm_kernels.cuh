@@ -9,6 +9,7 @@ struct tm_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     int num_sms = 0;
+    unsigned probe = 0;            // TM_PROBE_* flags for objects created from now on (tests)
 };
 
 namespace tmg {
@@ -46,6 +47,7 @@ struct DornicArgs {
     int rows_cap;                  // rows of the largest task (<= kMaxRowsPerTask)
     const T* site_b;               // per-site loss coefficient b_v (packed like the state) or nullptr
     int zero_fixed;                // a +0 draw finishes as +0, no status bit (finite b, c, dt; no site_b)
+    int cap1;                      // TM_PROBE_SAMPLER_CAP1: rejection loops stop after one attempt
 };
 
 template <typename T>
@@ -57,6 +59,8 @@ struct RK4Args {
     const int4* tasks;             // block tasks
     int n_tasks;
     T alpha, k2, k2W0, gmax, cgmax, k1, rW, d, DPx, DWx, DOx, dt2, dt6, dt, clo, ceps;
+    int wait_limit;                // polls of a tile's copy barrier before the CTA gives up
+    int probe_no_copy;             // TM_PROBE_TILE_WAIT: issue no copy, so the bounded wait runs out
 };
 
 template <typename T>
@@ -74,6 +78,9 @@ cudaError_t launch_rk4(const RK4Args<T>& a, bool det, int grid, cudaStream_t s);
 template <typename T>
 cudaError_t launch_measure(const T* state, const InstTables& it, const int4* tasks, int n_tasks, int nf,
                            double* partial, int grid, int block, cudaStream_t s);
+template <typename T>
+cudaError_t launch_validate(const T* state, const InstTables& it, const int4* tasks, int n_tasks, int nf, int grid,
+                            cudaStream_t s);
 cudaError_t launch_finalize(const double* partial, const int* task_begin, const InstTables& it, int n_inst, int nf,
                             int dp_extinction, double* obs_row, cudaStream_t s);
 cudaError_t launch_consts(const double* a0, const double* astep, int n, double diff4, double sigma2, double dt,

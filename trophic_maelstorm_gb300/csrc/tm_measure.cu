@@ -117,6 +117,46 @@ template cudaError_t launch_measure<float>(const float*, const InstTables&, cons
 template cudaError_t launch_measure<double>(const double*, const InstTables&, const int4*, int, int, double*, int,
                                             int, cudaStream_t);
 
+// Status bits of an uploaded state, per instance: TM_STATUS_NAN_BIT for a NaN or
+// Inf and TM_STATUS_NEG_BIT for a negative value in any field -- the checks the
+// reference runs on every new state (multiSPDP.cpp:2949-2955, 3237-3255;
+// rietkerk_bjork_FKE.cpp:4352-4370), applied to the state a caller uploads.
+template <typename T>
+__global__ void __launch_bounds__(256) validate_kernel(const T* state, const InstTables it, const int4* tasks,
+                                                       int n_tasks, int nf)
+{
+    const int lane = threadIdx.x & 31;
+    const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int nw = (int)((gridDim.x * blockDim.x) >> 5);
+    for (int t = gw; t < n_tasks; t += nw) {
+        const int4 tk = tasks[t];
+        const int k = tk.x;
+        const int L = it.L[k];
+        const int x = tk.y + lane;
+        unsigned st = 0;
+        if (x < L) {
+            const T* base = state + it.off[k];
+            const long long fs = it.fstride[k];
+            for (int r = 0; r < tk.w; ++r)
+                for (int f = 0; f < nf; ++f) st |= value_status(base[f * fs + (long long)(tk.z + r) * L + x]);
+        }
+        st = __reduce_or_sync(0xffffffffu, st);
+        if (lane == 0 && st) atomicOr(it.status + k, st);
+    }
+}
+
+template <typename T>
+cudaError_t launch_validate(const T* state, const InstTables& it, const int4* tasks, int n_tasks, int nf, int grid,
+                            cudaStream_t s)
+{
+    if (n_tasks <= 0) return cudaSuccess;
+    validate_kernel<T><<<grid, 256, 0, s>>>(state, it, tasks, n_tasks, nf);
+    return cudaGetLastError();
+}
+template cudaError_t launch_validate<float>(const float*, const InstTables&, const int4*, int, int, int, cudaStream_t);
+template cudaError_t launch_validate<double>(const double*, const InstTables&, const int4*, int, int, int,
+                                             cudaStream_t);
+
 // One warp per instance: obs_row[k*W + f], W = 2 (DP: mean, active) or 4
 // (Rietkerk: mean P, W, O, active P).  With dp_extinction, an instance seen with
 // no active site is marked extinct (stochasticSPDP.cpp:1021-1022).

@@ -19,7 +19,8 @@
 //     in tile order (no atomics: the result does not depend on scheduling) and
 //     applies Adam to the FP32 master weights, refreshing their BF16 copies.
 // Every wait on an MMA completion is bounded: on timeout the CTA records an
-// error, frees its TMEM and returns.
+// error, waits once more (again bounded) for the MMAs it issued, frees its
+// TMEM and returns; the update kernel then leaves the parameters unchanged.
 #include "tm_kernels.cuh"
 #include "../../include/tm.h"
 
@@ -58,6 +59,7 @@ static_assert(TS * FPAD * 4 <= 3 * BUF, "scratch fits buffers 0-2");
 static_assert(SM_BAR % 8 == 0, "mbarrier alignment");
 
 constexpr int kWaitLimit = 1 << 22;  // polls of an MMA completion before the CTA gives up (~0.3 s)
+constexpr int kProbeWaitLimit = 1 << 16;  // the same under TM_PROBE_MLP_WAIT (nothing in flight)
 
 // byte offset of element (row r, k) of a 128-row operand in the K-major,
 // no-swizzle canonical layout: 8 x 16-byte core matrices, 128 B apart along K
@@ -105,9 +107,9 @@ __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity)
+__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity, int limit)
 {
-    for (int i = 0; i < kWaitLimit; ++i) {
+    for (int i = 0; i < limit; ++i) {
         uint32_t ok;
         asm volatile("{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
                      "selp.u32 %0, 1, 0, p;\n\t}\n"
@@ -195,6 +197,8 @@ struct MlpArgs {
     float* loss_part;                // [tiles] partial losses (training)
     float* y_out;                    // n x 2 outputs (inference)
     int* err;                        // set to 1 when an MMA wait ran out
+    int wait_limit;                  // polls of one MMA completion
+    int probe_no_mma;                // TM_PROBE_MLP_WAIT: the first GEMM is not issued, so its wait runs out
 };
 
 template <bool TRAIN>
@@ -284,12 +288,12 @@ __global__ void __launch_bounds__(NT, 1) mlp_tile_kernel(MlpArgs a)
         }
         fence_async_smem();
         __syncthreads();
-        if (tid == 0) {
+        if (tid == 0 && !a.probe_no_mma) {
             tc_fence_after();
             mma_128(tmem + 0, saddr(B2), saddr(B0));          // a2 - b2 -> TMEM cols 0..127
             mma_commit(bar_a);
         }
-        failed = __syncthreads_or(!bar_wait(bar_a, phase));
+        failed = __syncthreads_or(!bar_wait(bar_a, phase, a.wait_limit));
         phase ^= 1;
         if (failed) break;
         tc_fence_after();
@@ -314,7 +318,7 @@ __global__ void __launch_bounds__(NT, 1) mlp_tile_kernel(MlpArgs a)
             mma_128(tmem + 128, saddr(B2), saddr(B1));        // a3 - b3 -> TMEM cols 128..255
             mma_commit(bar_a);
         }
-        failed = __syncthreads_or(!bar_wait(bar_a, phase));
+        failed = __syncthreads_or(!bar_wait(bar_a, phase, a.wait_limit));
         phase ^= 1;
         if (failed) break;
         tc_fence_after();
@@ -427,7 +431,7 @@ __global__ void __launch_bounds__(NT, 1) mlp_tile_kernel(MlpArgs a)
             mma_commit(bar_a);
         }
         red[(cs * TS + t) * 3 + 2] = row_sum_part(B5, t, cs);   // gb3 partial: row t of dz3^T, samples 32 cs..
-        failed = __syncthreads_or(!bar_wait(bar_a, phase));
+        failed = __syncthreads_or(!bar_wait(bar_a, phase, a.wait_limit));
         phase ^= 1;
         if (failed) break;
         tc_fence_after();
@@ -470,7 +474,7 @@ __global__ void __launch_bounds__(NT, 1) mlp_tile_kernel(MlpArgs a)
             mma_commit(bar_a);
         }
         red[(cs * TS + t) * 3 + 2] = row_sum_part(B5, t, cs);   // gb2 partial
-        failed = __syncthreads_or(!bar_wait(bar_a, phase));
+        failed = __syncthreads_or(!bar_wait(bar_a, phase, a.wait_limit));
         phase ^= 1;
         if (failed) break;
         tc_fence_after();
@@ -524,7 +528,12 @@ __global__ void __launch_bounds__(NT, 1) mlp_tile_kernel(MlpArgs a)
         }
     } while (false);
 
-    if (failed && tid == 0) atomicExch(a.err, 1);
+    if (failed) {
+        // the wait on the phase just toggled past ran out: give the MMAs issued
+        // for it one more bounded wait before their TMEM is freed
+        if (tid == 0) atomicExch(a.err, 1);
+        (void)bar_wait(bar_a, phase ^ 1u, a.wait_limit);
+    }
     tc_fence_before();
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" :: "r"(tmem) : "memory");
@@ -544,10 +553,12 @@ struct AdamArgs {
     int update;
     float lr, b1, b2, eps, c1, c2;
     __nv_bfloat16 *W2, *W2T, *W3, *W3T;
+    const int* err;                  // a tile kernel's wait ran out: the partials are invalid, change nothing
 };
 
 __global__ void mlp_adam_kernel(AdamArgs a)
 {
+    if (a.err != nullptr && *a.err != 0) return;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < NP; i += gridDim.x * blockDim.x) {
         float pv = a.p[i];
         if (a.n_tiles > 0) {
@@ -665,6 +676,7 @@ AdamArgs adam_args(tm_mlp* m, int n_tiles, double* loss_out, float* grad_out, in
     a.W2T = m->W2T;
     a.W3 = m->W3;
     a.W3T = m->W3T;
+    a.err = m->err;
     return a;
 }
 
@@ -685,6 +697,8 @@ MlpArgs tile_args(tm_mlp* m, const float* x, int n, float inv_norm, float* y_out
     a.loss_part = m->loss_part;
     a.y_out = y_out;
     a.err = m->err;
+    a.probe_no_mma = (m->ctx->probe & TM_PROBE_MLP_WAIT) ? 1 : 0;
+    a.wait_limit = a.probe_no_mma ? kProbeWaitLimit : kWaitLimit;
     return a;
 }
 
@@ -847,9 +861,9 @@ int tm_mlp_train(tm_mlp* m, int steps, float lr, float beta1, float beta2, float
         AdamArgs a = adam_args(m, tiles, m->loss_dev + k, nullptr, 1, lr, beta1, beta2, eps, c1, c2);
         mlp_adam_kernel<<<(NP + 255) / 256, 256, 0, s>>>(a);
     }
-    m->step += steps;
     const int rc = finish(m);
     if (rc != TM_OK) return rc;
+    m->step += steps;
     if (loss_hist && steps > 0)
         MLP_CUDA(cudaMemcpy(loss_hist, m->loss_dev, (size_t)steps * sizeof(double), cudaMemcpyDeviceToHost));
     return TM_OK;

@@ -60,13 +60,19 @@ __device__ __forceinline__ void rk_rhs_cell(const RK4Args<T>& A, const T* S, int
 // starting on a 16-byte boundary (instance offsets and field strides are
 // multiples of 32 elements), so one thread issues them as cp.async.bulk copies
 // completing on an mbarrier instead of 256 threads loading 5184 values.
-constexpr int kRkWaitLimit = 1 << 22;   // polls of the tile's copies before the CTA gives up
+// Every wait on the copies is bounded (RK4Args::wait_limit polls, about 0.3 s at
+// the default): a CTA whose copies do not complete marks the instances of its
+// current and remaining tiles with TM_STATUS_WAIT_BIT (their fields are invalid
+// after this step, and the host call returns TM_ERR_TIMEOUT), waits once more,
+// again bounded, for copies still in flight into its shared memory, and exits.
+// Under TM_PROBE_TILE_WAIT the CTA issues no copy and arms nothing, so the
+// first wait runs out with nothing in flight (the test of this path).
 
 __device__ __forceinline__ uint32_t rk_saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-__device__ __forceinline__ bool rk_bar_wait(uint32_t bar, uint32_t parity)
+__device__ __forceinline__ bool rk_bar_wait(uint32_t bar, uint32_t parity, int limit)
 {
-    for (int i = 0; i < kRkWaitLimit; ++i) {
+    for (int i = 0; i < limit; ++i) {
         uint32_t ok;
         asm volatile("{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
                      "selp.u32 %0, 1, 0, p;\n\t}\n"
@@ -115,10 +121,11 @@ __global__ void __launch_bounds__(RK_THREADS, (sizeof(T) == 4 ? RK_CTAS : 1)) rk
             // one halo row per thread (3 x RK_RY rows): the block takes the bulk path
             // only if every row start is 16-byte aligned
             constexpr int kRows = 3 * RK_RY;
-            const bool shape = sizeof(T) == 4 && one_wrap && (L & 3) == 0 && x0 >= RK_H && x0 + RK_TX + RK_H <= L;
+            const bool shape = (sizeof(T) == 4 && one_wrap && (L & 3) == 0 && x0 >= RK_H && x0 + RK_TX + RK_H <= L) ||
+                               A.probe_no_copy;
             const T* src = nullptr;
             bool aligned = true;
-            if (shape && tid < kRows) {
+            if (shape && !A.probe_no_copy && tid < kRows) {
                 const int f = tid / RK_RY, ry = tid - f * RK_RY;
                 int gy = y0 - RK_H + ry;
                 gy = gy < 0 ? gy + L : (gy >= L ? gy - L : gy);
@@ -126,7 +133,7 @@ __global__ void __launch_bounds__(RK_THREADS, (sizeof(T) == 4 ? RK_CTAS : 1)) rk
                 aligned = ((uintptr_t)src & 15u) == 0;
             }
             const bool bulk = shape && __syncthreads_and(aligned);
-            if (bulk) {
+            if (bulk && !A.probe_no_copy) {
                 constexpr uint32_t row_bytes = RK_RX * sizeof(T);
                 static_assert((RK_RX * sizeof(float)) % 16 == 0 && (RK_RN * sizeof(float)) % 16 == 0, "bulk rows");
                 if (tid == 0)
@@ -146,10 +153,14 @@ __global__ void __launch_bounds__(RK_THREADS, (sizeof(T) == 4 ? RK_CTAS : 1)) rk
         }
         __syncthreads();
         if (tile_bulk) {
-            const bool ok = rk_bar_wait(bar, phase);
+            const bool ok = rk_bar_wait(bar, phase, A.wait_limit);
             phase ^= 1u;
-            if (__syncthreads_or(!ok)) {          // copies did not complete: report and stop
-                if (tid == 0) atomicOr(A.it.status + k, TM_STATUS_CAP_BIT);
+            if (__syncthreads_or(!ok)) {
+                // copies did not complete: flag this tile's and every later tile's
+                // instance, give copies still in flight one more bounded wait, stop
+                for (int t2 = t + tid * (int)gridDim.x; t2 < A.n_tasks; t2 += RK_THREADS * (int)gridDim.x)
+                    atomicOr(A.it.status + A.tasks[t2].x, TM_STATUS_WAIT_BIT);
+                (void)rk_bar_wait(bar, phase ^ 1u, A.wait_limit);
                 return;
             }
         } else

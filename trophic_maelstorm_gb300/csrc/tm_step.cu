@@ -75,13 +75,13 @@ __device__ __forceinline__ T finish_site(const DornicArgs<T>& A, T rs, T bi, uns
 // One site through the general sampler, then finished and stored.  The draw
 // depends only on (seed, site, step), so it may run in any later pass of the
 // same warp.
-template <typename T, int REM, int SAMP>
+template <typename T, int REM, int SAMP, int CAP>
 __device__ __forceinline__ void draw_general_site(const DornicArgs<T>& A, const SmemTab<T>& tab, long long step,
                                                   int k, uint32_t site, T m, T mu1)
 {
     Stream<T> g;
     g.init(A.it.seed[k], site, step);
-    const T rs = dornic_draw(g, m, mu1, (T)A.it.consts[k].y, SAMP, tab);
+    const T rs = dornic_draw<CAP>(g, m, mu1, (T)A.it.consts[k].y, SAMP, tab);
     const long long o = A.it.off[k] + (long long)site;
     unsigned st = g.status;
     A.out[o] = finish_site<T, REM>(A, rs, A.site_b ? A.site_b[o] : A.b, st);
@@ -90,8 +90,11 @@ __device__ __forceinline__ void draw_general_site(const DornicArgs<T>& A, const 
 
 // SAMP is the sampler (0 exact, 1 Gaussian above 100, 2 noise off) as a
 // compile-time constant: each instantiation carries only its own sampler's
-// code, which keeps the loop body small for the instruction cache.
-template <typename T, int REM, int SAMP>
+// code, which keeps the loop body small for the instruction cache.  CAP is the
+// attempts of each rejection loop: kSamplerCap, or 1 in the instantiation that
+// TM_PROBE_SAMPLER_CAP1 selects (the straight-line draw makes one attempt of
+// each loop, so it is unchanged).
+template <typename T, int REM, int SAMP, int CAP>
 __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_kernel(const DornicArgs<T> A)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -255,7 +258,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
                     me = Wqm[j];
                     mue = Wqmu[j];
                 }
-                draw_general_site<T, REM, SAMP>(A, tab, step, ke, se, me, mue);
+                draw_general_site<T, REM, SAMP, CAP>(A, tab, step, ke, se, me, mue);
             }
         }
         if (!more) break;
@@ -275,24 +278,28 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
     }
 }
 
-template <typename T, int REM, int SAMP>
+template <typename T, int REM, int SAMP, int CAP = kSamplerCap>
 cudaError_t launch_dornic_t(const DornicArgs<T>& a, int grid, int block, size_t smem, cudaStream_t s)
 {
     static bool attr_set = false;
     if (!attr_set) {
         const int full = (int)(warp_scratch_bytes<T>(kMaxRowsPerTask) * kWarps);
-        const cudaError_t e =
-            cudaFuncSetAttribute(dornic_step_kernel<T, REM, SAMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, full);
+        const cudaError_t e = cudaFuncSetAttribute(dornic_step_kernel<T, REM, SAMP, CAP>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, full);
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
-    dornic_step_kernel<T, REM, SAMP><<<grid, block, smem, s>>>(a);
+    dornic_step_kernel<T, REM, SAMP, CAP><<<grid, block, smem, s>>>(a);
     return cudaGetLastError();
 }
 
 template <typename T, int REM>
 cudaError_t launch_dornic_r(const DornicArgs<T>& a, int grid, int block, size_t smem, cudaStream_t s)
 {
+    if (a.cap1) {  // the sampler-cap probe: DP, Euler-exact remainder, exact sampler only
+        if (REM == 0 && a.sampler == 0) return launch_dornic_t<T, 0, 0, 1>(a, grid, block, smem, s);
+        return cudaErrorInvalidValue;
+    }
     if (a.sampler == 0) return launch_dornic_t<T, REM, 0>(a, grid, block, smem, s);
     if (a.sampler == 1) return launch_dornic_t<T, REM, 1>(a, grid, block, smem, s);
     if (a.sampler == 2) return launch_dornic_t<T, REM, 2>(a, grid, block, smem, s);
