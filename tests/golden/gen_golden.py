@@ -21,11 +21,21 @@ ref_dp_ensemble.npz  per-replicate trajectories of percolationDornic_2D
                    reference seeds std::mt19937_64 from std::random_device, so
                    these draws are not reproducible; they are a fixed sample of
                    the reference's ensemble, compared statistically.
+ref_spectrum.npz   radially averaged power spectra computed by the reference's own
+                   gen_FFT_PowerSpectra (glow_up.py:632-847, run through
+                   glow_up_harness.py) on frame files written by the reference's
+                   save_frame; each case keeps the field as the estimator read it
+                   (save_frame prints 6 significant digits), k and the power
+                   (NaN where the reference leaves a bin empty).
+ref_lnspace.npz    the reference's lnspace<int> (stochasticSPDP.cpp:281-301), which picks
+                   the lattice sides of the stationary finite-size sweep.
 ref_libstdcxx.npz  draws of the libstdc++ poisson_distribution / gamma_distribution
                    the reference's Dornic step constructs (stochasticSPDP.cpp:1055-1059),
                    from a seeded std::mt19937_64, alone and composed as the step's whole
                    draw Gamma(mu1 + Poisson(m)).
 
+    python tests/golden/gen_golden.py --spectrum   # only ref_spectrum.npz (needs TM_REF_ROOT)
+    python tests/golden/gen_golden.py --lnspace    # only ref_lnspace.npz
     python tests/golden/gen_golden.py --fke        # only ref_fke.npz
     python tests/golden/gen_golden.py --libstdcxx  # only ref_libstdcxx.npz
 """
@@ -199,6 +209,78 @@ def fke(libs, rng):
     return out
 
 
+LNSPACE_CASES = ((32, 1024, 6), (40, 400, 10), (31, 257, 7), (64, 64, 1), (50, 200, 4), (33, 1000, 25))
+
+
+def lnspace_cases():
+    lib = C.CDLL(os.path.join(REF, "libref_lnspace.so"))
+    lib.ref_lnspace.argtypes = [C.c_int, C.c_int, C.c_int, dp, C.c_int]
+    out = {}
+    for k, (a, b, n) in enumerate(LNSPACE_CASES):
+        buf = np.zeros(64)
+        m = lib.ref_lnspace(a, b, n, _p(buf), 64)
+        out[f"lnspace_{k}"] = buf[:m].copy()
+    out["cases"] = np.array(LNSPACE_CASES)
+    return out
+
+
+def spectrum_frames(rng):
+    """Fields of the power-spectrum fixture: stripes, an odd side, spots with an
+    empty region, an all-zero lattice (no power: every bin empty) and a
+    three-cosine pattern."""
+    out = {}
+    L = 32
+    y, x = np.mgrid[0:L, 0:L]
+    out["stripes32"] = 1.0 + 0.5 * np.sin(2 * np.pi * x / 8.0) + 0.05 * rng.random((L, L))
+    out["random33"] = rng.uniform(0, 2, (33, 33))
+    L = 48
+    y, x = np.mgrid[0:L, 0:L]
+    f = (1.0 + np.cos(2 * np.pi * x / 12.0)) * (1.0 + np.cos(2 * np.pi * y / 6.0)) + 0.1 * rng.random((L, L))
+    f[:10, :14] = 0.0
+    out["spots48"] = f
+    out["zeros20"] = np.zeros((20, 20))
+    L = 64
+    y, x = np.mgrid[0:L, 0:L]
+    q = 2 * np.pi / 16.0
+    f = sum(np.cos(q * (np.cos(th) * x + np.sin(th) * y)) for th in (0.0, 2 * np.pi / 3, 4 * np.pi / 3))
+    out["hex64"] = np.maximum(f, 0.0) + 0.02 * rng.random((L, L))
+    return out
+
+
+def spectrum(libs, rng):
+    """gen_FFT_PowerSpectra of the reference on frames written by the reference's
+    save_frame (one field per file, header of the reference's DP frames)."""
+    import shutil
+    import tempfile
+    sys.path.insert(0, HERE)
+    import glow_up_harness as gh
+    ref_root = os.environ.get("TM_REF_ROOT")
+    if not ref_root:
+        sys.exit("set TM_REF_ROOT to the reference checkout")
+    out = {}
+    d = tempfile.mkdtemp()
+    home = tempfile.mkdtemp()
+    try:
+        gu = gh.load_glow_up(ref_root, home)
+        for name, f in spectrum_frames(rng).items():
+            L = f.shape[0]
+            sub = os.path.join(d, name)
+            os.makedirs(sub)
+            pat = "/FRAME_T_100_a_0.9_R_"
+            libs["multisp"].ref_save_frame(_p(np.ascontiguousarray(f.ravel())), L, sub.encode(), pat.encode(), 0.9, 0,
+                                           "a_c,  x,  P(x; t) \n".encode())
+            path = f"{sub}{pat}0.csv"
+            read = gh.read_csv(path)
+            k, p = gh.spectrum_of_frame(gu, path)
+            out[f"{name}_field"] = read[read.columns[2]].values.reshape(L, L)
+            out[f"{name}_k"], out[f"{name}_power"] = k, p
+        out["names"] = np.array(list(spectrum_frames(np.random.default_rng(0)).keys()))
+    finally:
+        shutil.rmtree(d)
+        shutil.rmtree(home)
+    return out
+
+
 # means and shapes of the sampler-level comparison with libstdc++
 LIBSTDCXX_POISSON = (0.3, 3.0, 17.0, 50.0, 250.0)
 LIBSTDCXX_GAMMA = (0.4, 1.7, 8.0, 60.0)
@@ -231,11 +313,20 @@ def main():
     if "--libstdcxx" in sys.argv:
         np.savez_compressed(os.path.join(HERE, "ref_libstdcxx.npz"), **libstdcxx(load(("dp",))))
         return
+    if "--lnspace" in sys.argv:
+        np.savez_compressed(os.path.join(HERE, "ref_lnspace.npz"), **lnspace_cases())
+        return
+    if "--spectrum" in sys.argv:
+        np.savez_compressed(os.path.join(HERE, "ref_spectrum.npz"),
+                            **spectrum(load(("dp", "rietkerk", "multisp")), np.random.default_rng(5)))
+        return
     if "--fke" in sys.argv:
         np.savez_compressed(os.path.join(HERE, "ref_fke.npz"), **fke(load(("fke",)), np.random.default_rng(11)))
         return
     import subprocess
     subprocess.run([sys.executable, os.path.abspath(__file__), "--fke"], check=True)
+    subprocess.run([sys.executable, os.path.abspath(__file__), "--spectrum"], check=True)
+    subprocess.run([sys.executable, os.path.abspath(__file__), "--lnspace"], check=True)
     libs = load()
     rng = np.random.default_rng(20261203)
     np.savez_compressed(os.path.join(HERE, "ref_pins.npz"), **pins(libs, rng))

@@ -5,6 +5,7 @@ import subprocess
 
 import numpy as np
 import pytest
+from spectrum_restatement import spectrum_numpy
 
 pytestmark = pytest.mark.gpu
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -23,25 +24,27 @@ def ctx(tmg):
     return tmg.Context(0)
 
 
-def spectrum_numpy(img, binwidth=0.5):
-    """gen_FFT_PowerSpectra (glow_up.py:752-827) for one column, restated with numpy:
-    max-normalise, |fft2|^2, radial bins from 1 - w/2 with np.histogram, mean x area."""
-    L = img.shape[0]
-    img = img.astype(np.float64)
-    mx = img.max()
-    img = img / (mx if mx != 0.0 else 1.0)
-    kbins = np.arange(1 - binwidth / 2, L // 2 + 1, binwidth)
-    kvals = 0.5 * (kbins[1:] + kbins[:-1])
-    F = np.fft.fft2(img)
-    kf = np.fft.fftfreq(L) * L
-    kx, ky = np.meshgrid(kf, kf)
-    knrm = np.sqrt(kx ** 2 + ky ** 2).flatten()
-    amp = np.abs(F ** 2).flatten()
-    s, _ = np.histogram(knrm, bins=kbins, weights=amp)
-    c, _ = np.histogram(knrm, bins=kbins)
-    p = np.divide(s, c, out=np.zeros_like(s), where=c != 0)
-    p *= np.pi * (kbins[1:] ** 2 - kbins[:-1] ** 2)
-    return kvals, p
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32"])
+@pytest.mark.parametrize("case", ["stripes32", "random33", "spots48", "zeros20", "hex64"])
+def test_power_spectrum_matches_reference_estimator(tmg, ctx, precision, case):
+    """Against the reference's own gen_FFT_PowerSpectra (glow_up.py:632-847), run on
+    frames written by its save_frame (tests/golden/ref_spectrum.npz).  Empty bins:
+    NaN there, 0 here.  FP64 state: 1e-9 of the largest power; FP32 state rounds the
+    field once (2^-24 relative), so 2e-6."""
+    g = np.load(os.path.join(REPO, "tests", "golden", "ref_spectrum.npz"))
+    f, rk, rp = g[f"{case}_field"], g[f"{case}_k"], g[f"{case}_power"]
+    L = f.shape[0]
+    dtype = np.float64 if precision == 0 else np.float32
+    b = tmg.Batch(ctx, tmg.dp_model(), tmg.instances([L], [0], 0.72), precision)
+    b.upload([f.astype(dtype)])
+    kv, pw = b.power_spectrum(0)
+    b.close()
+    np.testing.assert_allclose(kv, rk, rtol=0, atol=1e-12)
+    want = np.nan_to_num(rp, nan=0.0)
+    tol = 1e-9 if precision == 0 else 2e-6
+    np.testing.assert_allclose(pw, want, rtol=tol, atol=tol * max(1.0, want.max()))
+    if np.isfinite(rp).any():
+        assert tmg.pattern_wavelength(L, kv, pw) == pytest.approx(L / rk[np.nanargmax(rp)])
 
 
 @pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32"])

@@ -1,5 +1,7 @@
 """The oracle against the reference's own code (golden fixtures made by
 tests/golden/gen_golden.py from the compiled reference sources)."""
+import os
+
 import numpy as np
 import pytest
 from scipy import stats
@@ -122,3 +124,15 @@ def test_fke_advdiff_matches_reference(oracle, golden, tag):
     # mass is conserved up to the sites below eps, which the reference drops
     rho = g[f"fke_{tag}_rho"]
     assert out.sum() == pytest.approx(rho[rho >= 1e-10].sum(), rel=1e-12)
+
+
+def test_spectrum_restatement_matches_reference_estimator():
+    """The numpy restatement the GPU spectrum tests also use equals the reference's
+    gen_FFT_PowerSpectra output (empty bins: NaN there, 0 here)."""
+    from spectrum_restatement import spectrum_numpy
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_spectrum.npz"))
+    for case in g["names"]:
+        k, p = spectrum_numpy(g[f"{case}_field"])
+        np.testing.assert_array_equal(k, g[f"{case}_k"])
+        want = np.nan_to_num(g[f"{case}_power"], nan=0.0)
+        np.testing.assert_allclose(p, want, rtol=1e-12, atol=1e-12 * max(1.0, want.max()))
