@@ -65,8 +65,7 @@ struct tm_batch {
 
     void* buf[2] = {nullptr, nullptr};
     int cur = 0;
-    void* aux = nullptr;        // Rietkerk P* (field-0 slots) / noise-off DP stage buffers
-    void* kst[4] = {nullptr, nullptr, nullptr, nullptr};
+    void* aux = nullptr;        // Rietkerk P* (field-0 slots)
     void* site_b = nullptr;     // per-site loss coefficient (DP), packed like the state
     long long* d_step = nullptr;
     int64_t step = 0;
@@ -156,8 +155,8 @@ int build_tasks(tm_batch* b)
     TM_CUDA(cudaMemcpy(b->d_tasks, tasks.data(), tasks.size() * sizeof(int4), cudaMemcpyHostToDevice));
     if (!b->d_task_begin) TM_CUDA(dalloc(&b->d_task_begin, begin.size()));
     TM_CUDA(cudaMemcpy(b->d_task_begin, begin.data(), begin.size() * sizeof(int), cudaMemcpyHostToDevice));
-    // RK4 tiles
-    if (b->model == 1 && !b->d_btasks) {
+    // 64 x 32 tiles (Rietkerk RK4, noise-off DP)
+    if ((b->model == 1 || b->dpm.deterministic) && !b->d_btasks) {
         std::vector<int4> bt;
         for (int k = 0; k < b->n_inst; ++k) {
             const int L = b->inst[k].L;
@@ -238,30 +237,15 @@ cudaError_t enqueue_step_t(tm_batch* b, int src_idx, const long long* step_base,
     if (b->model == 0) {
         const tm_dp_model& m = b->dpm;
         if (m.deterministic) {
-            // noise-off lattice RK4 / Euler, instance by instance
-            const int nst = m.integrator ? 4 : 1;
-            for (int k = 0; k < b->n_inst && e == cudaSuccess; ++k) {
-                const long long o = b->off[k];
-                const int L = b->inst[k].L;
-                for (int st = 0; st < nst && e == cudaSuccess; ++st) {
-                    DetStageArgs<T> d{};
-                    d.x0 = in + o;
-                    d.kprev = st == 0 ? nullptr : (const T*)b->kst[st - 1] + o;
-                    d.kout = (T*)b->kst[st] + o;
-                    d.L = L;
-                    d.coef = (T)(st == 3 ? m.dt : m.dt / 2.0);
-                    d.a = (T)b->inst[k].a; d.b = (T)m.b; d.c = (T)m.c;
-                    d.dlap = (T)(m.D / (m.dx * m.dx));
-                    d.dk12 = (T)(m.D * (1.0 / ((12.0 * m.dx) * m.dx)));
-                    d.cubic = (m.c != 0.0); d.stencil = m.stencil;
-                    e = launch_det_stage<T>(d, s);
-                }
-                if (e == cudaSuccess)
-                    e = launch_det_final<T>(in + o, (const T*)b->kst[0] + o, (const T*)b->kst[1] + o,
-                                            (const T*)b->kst[2] + o, (const T*)b->kst[3] + o, out + o,
-                                            (long long)L * L, (T)m.dt, (T)(m.dt / 6.0), m.integrator, s);
-            }
-            return e;
+            // noise-off lattice RK4 / Euler: one tile launch for every instance
+            DetTileArgs<T> d{};
+            d.in = in; d.out = out; d.it = b->tables(); d.tasks = b->d_btasks; d.n_tasks = b->n_btasks;
+            d.b = (T)m.b; d.c = (T)m.c; d.cubic = (m.c != 0.0);
+            d.dlap = (T)(m.D / (m.dx * m.dx));
+            d.dk12 = (T)(m.D * (1.0 / ((12.0 * m.dx) * m.dx)));
+            d.dt = (T)m.dt; d.dt2 = (T)(m.dt / 2.0); d.dt6 = (T)(m.dt / 6.0);
+            const int grid = std::max(1, std::min(b->n_btasks, b->ctx->num_sms * 2));
+            return launch_dp_det<T>(d, m.stencil, m.integrator, grid, s);
         }
         if (b->ramped) {
             e = launch_consts(b->d_a0, b->d_astep, b->n_inst, (4.0 * m.D) / (m.dx * m.dx), m.sigma * m.sigma, m.dt,
@@ -314,9 +298,8 @@ int ensure_graph(tm_batch* b, int parity)
 int run_steps(tm_batch* b, int64_t n)
 {
     cudaStream_t s = b->ctx->stream;
-    const bool graphs = !(b->model == 0 && b->dpm.deterministic);
     while (n > 0) {
-        if (graphs && n >= kGraphSteps) {
+        if (n >= kGraphSteps) {
             int rc = ensure_graph(b, b->cur);
             if (rc != TM_OK) return rc;
             TM_CUDA(launch_set_step(b->d_step, b->step, s));
@@ -499,7 +482,6 @@ int tm_batch_destroy(tm_batch* b)
     cudaStreamSynchronize(b->ctx->stream);
     free_graphs(b);
     cudaFree(b->buf[0]); cudaFree(b->buf[1]); cudaFree(b->aux); cudaFree(b->site_b);
-    for (auto p : b->kst) cudaFree(p);
     cudaFree(b->d_step); cudaFree(b->d_off); cudaFree(b->d_fstride); cudaFree(b->d_L); cudaFree(b->d_seed);
     cudaFree(b->d_R); cudaFree(b->d_a0); cudaFree(b->d_astep); cudaFree(b->d_consts); cudaFree(b->d_alive);
     cudaFree(b->d_status); cudaFree(b->d_tasks); cudaFree(b->d_task_begin); cudaFree(b->d_btasks);
@@ -535,10 +517,6 @@ int tm_batch_create_dp(tm_ctx* c, const tm_dp_model* m, const tm_instance* inst,
     b->ctx = c; b->model = 0; b->precision = precision; b->nf = 1; b->dpm = *m;
     for (int k = 0; k < n_inst; ++k) b->ramped = b->ramped || inst[k].a_step != 0.0;
     rc = batch_common_init(b, inst, n_inst);
-    if (rc == TM_OK && m->deterministic) {
-        for (int st = 0; st < 4 && rc == TM_OK; ++st)
-            if (!cuda_ok(cudaMalloc(&b->kst[st], (size_t)b->total * b->esize))) rc = TM_ERR_NOMEM;
-    }
     if (rc == TM_OK && !m->deterministic) {
         if (!cuda_ok(launch_consts(b->d_a0, b->d_astep, n_inst, (4.0 * m->D) / (m->dx * m->dx),
                                    m->sigma * m->sigma, m->dt, nullptr, 0, b->d_consts, c->stream)) ||

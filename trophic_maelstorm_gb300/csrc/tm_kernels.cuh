@@ -64,10 +64,14 @@ struct RK4Args {
 };
 
 template <typename T>
-struct DetStageArgs {              // noise-off DP stage (one instance per launch)
-    const T* x0; const T* kprev; T* kout;
-    int L; T coef;                 // stage input = x0 + coef * kprev
-    T a, b, c, dlap, dk12; int cubic, stencil;
+struct DetTileArgs {               // noise-off DP step over 64 x 32 tiles of every instance (a = it.R[k])
+    const T* in;
+    T* out;
+    InstTables it;
+    const int4* tasks;             // block tasks
+    int n_tasks;
+    T b, c, dlap, dk12, dt, dt2, dt6;
+    int cubic;
 };
 
 // launchers (defined in the kernel translation units)
@@ -89,10 +93,7 @@ cudaError_t launch_set_step(long long* d_step, long long v, cudaStream_t s);
 template <typename T>
 cudaError_t launch_box_means(const T* field, int L, int box, double* out, cudaStream_t s);
 template <typename T>
-cudaError_t launch_det_stage(const DetStageArgs<T>& a, cudaStream_t s);
-template <typename T>
-cudaError_t launch_det_final(const T* x0, const T* k1, const T* k2, const T* k3, const T* k4, T* out, long long n,
-                             T dt, T dt6, int rk4, cudaStream_t s);
+cudaError_t launch_dp_det(const DetTileArgs<T>& a, int stencil, int rk4, int grid, cudaStream_t s);
 
 constexpr int kMaxRowsPerTask = 16;
 constexpr int RK_TX = 64, RK_TY = 32, RK_H = 4;

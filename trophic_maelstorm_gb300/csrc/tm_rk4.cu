@@ -279,77 +279,144 @@ template cudaError_t launch_rk4<float>(const RK4Args<float>&, bool, int, cudaStr
 template cudaError_t launch_rk4<double>(const RK4Args<double>&, bool, int, cudaStream_t);
 
 // ---- noise-off DP: drho/dt = a rho - b rho^2 - c rho^3 + D Lap(rho) ---------------
-// 5-point Laplacian, or the 4th-order cross of fP_2D (stochasticSPDP.cpp:516-529)
-// written as f = react - D/(12 dx^2) (o2 - 16 o1 + 60 rho).  One thread per site;
-// the stage input x0 + coef*kprev is formed on the fly for the site and its
-// neighbours (percNoDiff_2D :594-626).
-template <typename T>
-__device__ __forceinline__ T det_in(const DetStageArgs<T>& A, long long i)
+// percNoDiff_2D (stochasticSPDP.cpp:549-662) with the 5-point Laplacian or the
+// 4th-order cross of fP_2D (:516-529), written as f = react - D/(12 dx^2)
+// (o2 - 16 o1 + 60 rho).  One CTA per 64 x 32 tile (persistent over the tiles of
+// every instance), all stages in shared memory as in rk4_tile_kernel: a stencil of
+// radius RAD makes stage s need stage s-1 values RAD sites further out, so the tile
+// loads a halo of NST * RAD sites and evaluates stage s on the region inset by
+// (s+1) RAD.  The reference keeps K1..K4 and the stage input as full lattices
+// (:594-626); here they never leave the SM, and one launch per step covers the
+// whole batch.
+template <typename T, int RAD>
+__device__ __forceinline__ T dp_det_rhs(const DetTileArgs<T>& A, const T* S, int c, int rx, T a)
 {
-    return A.kprev ? A.x0[i] + A.coef * A.kprev[i] : A.x0[i];
+    const T r = S[c];
+    T f = (a * r) - ((A.b * r) * r);
+    if (A.cubic) f = f - ((A.c * r) * r) * r;
+    if constexpr (RAD == 1) {
+        const T lap = (((S[c - rx] + S[c + rx]) + S[c - 1]) + S[c + 1]) - T(4) * r;
+        f = f + A.dlap * lap;
+    } else {
+        const T o2 = ((S[c - 2 * rx] + S[c + 2 * rx]) + S[c - 2]) + S[c + 2];
+        const T o1 = ((S[c - rx] + S[c + rx]) + S[c - 1]) + S[c + 1];
+        const T sm = (T(1) * o2 - T(16) * o1) + T(60) * r;
+        f = f - A.dk12 * sm;
+    }
+    return f;
 }
 
-template <typename T>
-__global__ void det_stage_kernel(const DetStageArgs<T> A)
+template <typename T, int RAD, int NST>
+__global__ void __launch_bounds__(RK_THREADS, 1) dp_det_tile_kernel(const DetTileArgs<T> A)
 {
-    const long long n = (long long)A.L * A.L;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const int L = A.L;
-        const int y = (int)(i / L), x = (int)(i - (long long)y * L);
-        const T r = det_in(A, i);
-        T f = (A.a * r) - ((A.b * r) * r);
-        if (A.cubic) f = f - ((A.c * r) * r) * r;
-        if (A.stencil == 5) {
-            const int yn = (y + L - 1) % L, ys = (y + 1) % L, xw = (x + L - 1) % L, xe = (x + 1) % L;
-            const T lap = (((det_in(A, (long long)yn * L + x) + det_in(A, (long long)ys * L + x)) +
-                            det_in(A, (long long)y * L + xw)) + det_in(A, (long long)y * L + xe)) - T(4) * r;
-            f = f + A.dlap * lap;
-        } else {
-            const int ym2 = (y + 2 * L - 2) % L, ym1 = (y + L - 1) % L, yp1 = (y + 1) % L, yp2 = (y + 2) % L;
-            const int xm2 = (x + 2 * L - 2) % L, xm1 = (x + L - 1) % L, xp1 = (x + 1) % L, xp2 = (x + 2) % L;
-            const T o2 = ((det_in(A, (long long)ym2 * L + x) + det_in(A, (long long)yp2 * L + x)) +
-                          det_in(A, (long long)y * L + xm2)) + det_in(A, (long long)y * L + xp2);
-            const T o1 = ((det_in(A, (long long)ym1 * L + x) + det_in(A, (long long)yp1 * L + x)) +
-                          det_in(A, (long long)y * L + xm1)) + det_in(A, (long long)y * L + xp1);
-            const T s = (T(1) * o2 - T(16) * o1) + T(60) * r;
-            f = f - A.dk12 * s;
+    constexpr int H = RAD * NST, RX = RK_TX + 2 * H, RY = RK_TY + 2 * H, RN = RX * RY;
+    constexpr int kPer = RK_TX * RK_TY / RK_THREADS;
+    extern __shared__ __align__(16) unsigned char det_smem[];
+    T* const X0 = reinterpret_cast<T*>(det_smem);
+    T* const MA = X0 + RN;
+    T* const MB = MA + RN;
+    const int tid = threadIdx.x;
+    for (int t = blockIdx.x; t < A.n_tasks; t += gridDim.x) {
+        const int4 tk = A.tasks[t];
+        const int k = tk.x;
+        const int L = A.it.L[k];
+        const long long off = A.it.off[k];
+        const T a = (T)A.it.R[k];
+        const int x0 = tk.y, y0 = tk.z;
+        const T* __restrict__ src = A.in + off;
+        __syncthreads();  // previous tile done with shared memory
+        const bool one_wrap = L >= RY && L >= RX;
+        for (int c = tid; c < RN; c += RK_THREADS) {
+            const int ry = c / RX, rx = c - ry * RX;
+            int gy = y0 - H + ry, gx = x0 - H + rx;
+            if (one_wrap) {
+                gy = gy < 0 ? gy + L : (gy >= L ? gy - L : gy);
+                gx = gx < 0 ? gx + L : (gx >= L ? gx - L : gx);
+            } else {
+                gy %= L; if (gy < 0) gy += L;
+                gx %= L; if (gx < 0) gx += L;
+            }
+            X0[c] = src[(long long)gy * L + gx];
         }
-        A.kout[i] = f;
+        __syncthreads();
+        T acc[kPer];
+#pragma unroll
+        for (int s = 0; s < NST; ++s) {
+            const T* S = (s == 0) ? X0 : ((s & 1) ? MA : MB);
+            T* D = (s & 1) ? MB : MA;
+            const T coef = (s == 2) ? A.dt : A.dt2;
+#pragma unroll
+            for (int j = 0; j < kPer; ++j) {
+                const int q = tid + j * RK_THREADS;
+                const int c = ((q / RK_TX) + H) * RX + (q % RK_TX) + H;
+                const T kv = dp_det_rhs<T, RAD>(A, S, c, RX, a);
+                if (s == 0) acc[j] = kv;
+                else if (s == NST - 1) acc[j] = acc[j] + kv;
+                else acc[j] = acc[j] + T(2) * kv;
+                if (s < NST - 1) D[c] = X0[c] + coef * kv;
+            }
+            if (s < NST - 1) {
+                // ring between the region inset by (s+1) RAD and the interior: top and
+                // bottom bands (tt rows of the inset's width w), left and right bands
+                const int in = (s + 1) * RAD, tt = H - in, w = RX - 2 * in;
+                const int nband = tt * w, nside = RK_TY * tt;
+                for (int q = tid; q < 2 * nband + 2 * nside; q += RK_THREADS) {
+                    int ry, rx;
+                    if (q < 2 * nband) {
+                        const int qb = q < nband ? q : q - nband;
+                        ry = (q < nband ? in : H + RK_TY) + qb / w;
+                        rx = in + qb % w;
+                    } else {
+                        const int qs = q - 2 * nband;
+                        const int qq = qs < nside ? qs : qs - nside;
+                        ry = H + qq / tt;
+                        rx = (qs < nside ? in : H + RK_TX) + qq % tt;
+                    }
+                    const int c = ry * RX + rx;
+                    D[c] = X0[c] + coef * dp_det_rhs<T, RAD>(A, S, c, RX, a);
+                }
+            }
+            __syncthreads();
+        }
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            const int q = tid + j * RK_THREADS;
+            const int ly = q / RK_TX, lx = q % RK_TX;
+            const int gy = y0 + ly, gx = x0 + lx;
+            if (gy < L && gx < L) {
+                const int c = (ly + H) * RX + lx + H;
+                const T v = (NST == 4) ? X0[c] + A.dt6 * acc[j] : X0[c] + acc[j] * A.dt;
+                A.out[off + (long long)gy * L + gx] = v;
+            }
+        }
     }
 }
 
-template <typename T>
-cudaError_t launch_det_stage(const DetStageArgs<T>& a, cudaStream_t s)
+template <typename T, int RAD, int NST>
+cudaError_t launch_det_t(const DetTileArgs<T>& a, int grid, cudaStream_t s)
 {
-    const long long n = (long long)a.L * a.L;
-    const int grid = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
-    det_stage_kernel<T><<<grid, 256, 0, s>>>(a);
-    return cudaGetLastError();
-}
-template cudaError_t launch_det_stage<float>(const DetStageArgs<float>&, cudaStream_t);
-template cudaError_t launch_det_stage<double>(const DetStageArgs<double>&, cudaStream_t);
-
-template <typename T>
-__global__ void det_final_kernel(const T* x0, const T* k1, const T* k2, const T* k3, const T* k4, T* out, long long n,
-                                 T dt, T dt6, int rk4)
-{
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        if (rk4) out[i] = x0[i] + dt6 * (((k1[i] + T(2) * k2[i]) + T(2) * k3[i]) + k4[i]);
-        else out[i] = x0[i] + k1[i] * dt;
+    constexpr int H = RAD * NST;
+    const size_t smem = 3 * (size_t)(RK_TX + 2 * H) * (RK_TY + 2 * H) * sizeof(T);
+    static bool attr = false;
+    if (!attr) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(dp_det_tile_kernel<T, RAD, NST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
     }
+    dp_det_tile_kernel<T, RAD, NST><<<grid, RK_THREADS, smem, s>>>(a);
+    return cudaGetLastError();
 }
 
 template <typename T>
-cudaError_t launch_det_final(const T* x0, const T* k1, const T* k2, const T* k3, const T* k4, T* out, long long n,
-                             T dt, T dt6, int rk4, cudaStream_t s)
+cudaError_t launch_dp_det(const DetTileArgs<T>& a, int stencil, int rk4, int grid, cudaStream_t s)
 {
-    const int grid = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
-    det_final_kernel<T><<<grid, 256, 0, s>>>(x0, k1, k2, k3, k4, out, n, dt, dt6, rk4);
-    return cudaGetLastError();
+    if (a.n_tasks <= 0) return cudaSuccess;
+    if (stencil == 5) return rk4 ? launch_det_t<T, 1, 4>(a, grid, s) : launch_det_t<T, 1, 1>(a, grid, s);
+    if (stencil == 9) return rk4 ? launch_det_t<T, 2, 4>(a, grid, s) : launch_det_t<T, 2, 1>(a, grid, s);
+    return cudaErrorInvalidValue;
 }
-template cudaError_t launch_det_final<float>(const float*, const float*, const float*, const float*, const float*,
-                                             float*, long long, float, float, int, cudaStream_t);
-template cudaError_t launch_det_final<double>(const double*, const double*, const double*, const double*,
-                                              const double*, double*, long long, double, double, int, cudaStream_t);
+template cudaError_t launch_dp_det<float>(const DetTileArgs<float>&, int, int, int, cudaStream_t);
+template cudaError_t launch_dp_det<double>(const DetTileArgs<double>&, int, int, int, cudaStream_t);
 
 }  // namespace tmg
