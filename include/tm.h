@@ -31,6 +31,7 @@
  */
 #ifndef TM_H
 #define TM_H
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -279,6 +280,20 @@ int tm_batch_power_spectrum(tm_batch* b, int k, int field, double binwidth, doub
 int tm_fke_advdiff_device(const void* dev_rho, const void* dev_gamma, const void* dev_vx, const void* dev_vy,
                           int precision, int L, double pref, double eps, const double* gD, int RD,
                           const double* gV, int RV, void* dev_out, void* stream);
+/* The same operator for a per-step consumer loop: the scratch is the caller's
+ * device workspace (tm_fke_workspace_bytes(precision, L) bytes, 256-byte
+ * aligned, reusable from call to call), the stencils travel in the launch
+ * arguments (RD, RV <= TM_FKE_WS_MAX_RADIUS), and the call only queues work on
+ * `stream`: it allocates nothing, copies nothing from the host and does not
+ * synchronise; dev_out is ready when the stream passes the call.  Two calls
+ * sharing one workspace must be ordered on the stream.  Results equal
+ * tm_fke_advdiff_device's bit for bit. */
+#define TM_FKE_WS_MAX_RADIUS 127
+size_t tm_fke_workspace_bytes(int precision, int L);
+int tm_fke_advdiff_device_ws(const void* dev_rho, const void* dev_gamma, const void* dev_vx, const void* dev_vy,
+                             int precision, int L, double pref, double eps, const double* gD, int RD,
+                             const double* gV, int RV, void* dev_out, void* dev_workspace, size_t workspace_bytes,
+                             void* stream);
 
 /* -- sweep surrogate: a small network trained on the integrator's own runs --
  * No counterpart in the reference, which locates the critical point by

@@ -248,6 +248,26 @@ def dp_batch_run_f32(params, Ls, seeds, fields, n_steps, n_threads=0):
     assert rc == 0
 
 
+_scatter = None
+
+
+def fke_scatter_lib():
+    """libtmo_fke_scatter.so: the reference's GPU scatter (updateMovement) restated,
+    for same-box comparisons with the library's gather (tmo_fke_scatter_f64)."""
+    global _scatter
+    if _scatter is None:
+        path = os.path.join(HERE, "_build", "libtmo_fke_scatter.so")
+        if not os.path.exists(path):
+            build()
+        L = C.CDLL(path)
+        vp = C.c_void_p
+        L.tmo_fke_scatter_f64.argtypes = [vp, vp, vp, vp, C.c_int, C.c_double, C.c_double, vp, C.c_int, vp, C.c_int,
+                                          vp, vp]
+        L.tmo_fke_scatter_f64.restype = C.c_int
+        _scatter = L
+    return _scatter
+
+
 def fke_advdiff(rho, gamma, vx, vy, pref, gD, gV, eps=1e-10):
     L = int(round(np.sqrt(rho.size)))
     a = [np.ascontiguousarray(x, np.float64).ravel() for x in (rho, gamma, vx, vy)]

@@ -210,6 +210,46 @@ def test_fke_advdiff_matches_oracle(tmg, oracle, L, v):
     assert got.sum() == pytest.approx(rho[rho >= 1e-10].sum(), rel=1e-12)
 
 
+@pytest.mark.parametrize("L", [9, 64, 256])
+def test_fke_workspace_entry_point_matches_and_reference_scatter_agrees(tmg, oracle, L):
+    """tm_fke_advdiff_device_ws on a reused workspace equals the allocating entry point
+    bit for bit (two calls in a row), and both agree with a restatement of the
+    reference's GPU scatter (updateMovement, FP64 atomics) to rounding."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(L + 1)
+    rho = rng.uniform(0, 3, (L, L))
+    rho[rng.random((L, L)) < 0.3] = 0.0
+    gam = rng.uniform(0, 1, (L, L))
+    vx = rng.uniform(-2.0, 2.0, (L, L))
+    vy = rng.uniform(-2.0, 2.0, (L, L))
+    p = tmg.fke_parameters(1.0, 2.0, 1.0, 1.2)
+    dev = torch.device("cuda", 0)
+    ts = [torch.as_tensor(x, dtype=torch.float64, device=dev) for x in (rho, gam, vx, vy)]
+    ws = tmg.api.fke_workspace(L)
+    a1 = tmg.fke_advdiff(*ts, p, workspace=ws).cpu().numpy()
+    a2 = tmg.fke_advdiff(*ts, p, workspace=ws).cpu().numpy()
+    ref = tmg.fke_advdiff(rho, gam, vx, vy, p)
+    assert np.array_equal(a1, ref) and np.array_equal(a2, ref)
+    lib = oracle.fke_scatter_lib()
+    gD = torch.as_tensor(p.gD, dtype=torch.float64, device=dev)
+    gV = torch.as_tensor(p.gV, dtype=torch.float64, device=dev)
+    out = torch.empty_like(ts[0])
+    s = torch.cuda.current_stream(dev)
+    assert lib.tmo_fke_scatter_f64(*(t.data_ptr() for t in ts), L, p.pref, 1e-10, gD.data_ptr(), len(p.gD) - 1,
+                                   gV.data_ptr(), len(p.gV) - 1, out.data_ptr(), s.cuda_stream) == 0
+    np.testing.assert_allclose(ref, out.cpu().numpy(), rtol=1e-12, atol=1e-14)
+    # the workspace entry point rejects a short or misaligned workspace
+    from trophic_maelstorm_gb300 import _lib as T
+    import ctypes as C
+    args = [t.data_ptr() for t in ts] + [T.TM_FP64, L, p.pref, 1e-10, np.ascontiguousarray(p.gD).ctypes.data_as(
+        C.POINTER(C.c_double)), len(p.gD) - 1, np.ascontiguousarray(p.gV).ctypes.data_as(C.POINTER(C.c_double)),
+        len(p.gV) - 1, out.data_ptr()]
+    need = T.lib().tm_fke_workspace_bytes(T.TM_FP64, L)
+    base = (ws.data_ptr() + 255) // 256 * 256
+    assert T.lib().tm_fke_advdiff_device_ws(*args, base, need - 1, s.cuda_stream) == T.TM_ERR_INVALID
+    assert T.lib().tm_fke_advdiff_device_ws(*args, base + 8, need, s.cuda_stream) == T.TM_ERR_INVALID
+
+
 @pytest.mark.parametrize("model,nf", [("multisp", 1), ("rietkerk", 3)])
 def test_sweep_driver_other_models(tmg, tmp_path, model, nf):
     """tm_sweep with the MultiSp DP and the Rietkerk models: the sweep table, one

@@ -19,6 +19,7 @@ TM_FP64, TM_FP32 = 0, 1
 TM_REM_EULER_EXACT, TM_REM_RK4 = 0, 1
 TM_SAMPLER_EXACT, TM_SAMPLER_REF_GAUSS100, TM_SAMPLER_OFF = 0, 1, 2
 TM_STENCIL_5, TM_STENCIL_9 = 5, 9
+TM_FKE_WS_MAX_RADIUS = 127
 
 # every symbol include/tm.h declares
 EXPORTS = (
@@ -32,6 +33,7 @@ EXPORTS = (
     "tm_batch_set_site_coeff", "tm_batch_box_means", "tm_fke_advdiff_device",
     "tm_mlp_create", "tm_mlp_destroy", "tm_mlp_set_params", "tm_mlp_get_params", "tm_mlp_set_data",
     "tm_mlp_loss_grad", "tm_mlp_train", "tm_mlp_predict", "tm_set_test_probe",
+    "tm_fke_workspace_bytes", "tm_fke_advdiff_device_ws",
 )
 
 
@@ -122,6 +124,9 @@ def lib():
             "tm_mlp_train": ([vp, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, dp], C.c_int),
             "tm_mlp_predict": ([vp, fp, C.c_int, fp], C.c_int),
             "tm_set_test_probe": ([vp, C.c_uint32], C.c_int),
+            "tm_fke_workspace_bytes": ([C.c_int, C.c_int], C.c_size_t),
+            "tm_fke_advdiff_device_ws": ([vp, vp, vp, vp, C.c_int, C.c_int, C.c_double, C.c_double, dp, C.c_int, dp,
+                                          C.c_int, vp, vp, C.c_size_t, vp], C.c_int),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)

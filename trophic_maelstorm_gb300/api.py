@@ -343,11 +343,24 @@ def fke_parameters(D, v, dt_adv, sigma, dx=1.0, CI=4):
     return FKEParams(pref, RD, RV, gaussian_stencil(sigma, RD), gaussian_stencil(sigma, RV))
 
 
-def fke_advdiff(rho, gamma, vx, vy, params: FKEParams, eps=1e-10, precision=T.TM_FP64, device=0):
+def fke_workspace(L, precision=T.TM_FP64, device=0):
+    """A device workspace for fke_advdiff(..., workspace=...) on L x L lattices
+    (tm_fke_workspace_bytes), allocated by torch, reusable for every step."""
+    import torch
+    n = int(T.lib().tm_fke_workspace_bytes(precision, int(L)))
+    if n == 0:
+        raise T.TMError(T.TM_ERR_INVALID, "fke_workspace: precision or L")
+    return torch.empty(n + 256, dtype=torch.uint8, device=torch.device("cuda", device))
+
+
+def fke_advdiff(rho, gamma, vx, vy, params: FKEParams, eps=1e-10, precision=T.TM_FP64, device=0, workspace=None):
     """One FKE advection-diffusion of a consumer field (advdiff_FKE_MultiSp,
     rietkerk_bjork_FKE.cpp:3614-3695) through tm_fke_advdiff_device.  rho, gamma,
     vx, vy are L x L arrays (numpy, or CUDA torch tensors of the precision's
-    dtype, which are used in place); returns the moved field in the same kind."""
+    dtype, which are used in place); returns the moved field in the same kind.
+    With workspace (fke_workspace) the call goes through tm_fke_advdiff_device_ws:
+    no allocation and no synchronisation inside the library (torch tensors in,
+    a torch tensor out, ready on the current stream)."""
     import torch
     dt = torch.float64 if precision == T.TM_FP64 else torch.float32
     as_numpy = isinstance(rho, np.ndarray)
@@ -362,10 +375,16 @@ def fke_advdiff(rho, gamma, vx, vy, params: FKEParams, eps=1e-10, precision=T.TM
     gV = np.ascontiguousarray(params.gV, np.float64)
     with torch.cuda.device(dev):
         s = torch.cuda.current_stream(dev)
-        T.check(T.lib().tm_fke_advdiff_device(*(t.data_ptr() for t in ts), precision, L, params.pref, eps,
-                                              gD.ctypes.data_as(C.POINTER(C.c_double)), len(gD) - 1,
-                                              gV.ctypes.data_as(C.POINTER(C.c_double)), len(gV) - 1,
-                                              out.data_ptr(), s.cuda_stream), "tm_fke_advdiff_device")
+        args = (*(t.data_ptr() for t in ts), precision, L, params.pref, eps,
+                gD.ctypes.data_as(C.POINTER(C.c_double)), len(gD) - 1, gV.ctypes.data_as(C.POINTER(C.c_double)),
+                len(gV) - 1, out.data_ptr())
+        if workspace is None:
+            T.check(T.lib().tm_fke_advdiff_device(*args, s.cuda_stream), "tm_fke_advdiff_device")
+        else:
+            base = workspace.data_ptr()
+            aligned = (base + 255) // 256 * 256
+            T.check(T.lib().tm_fke_advdiff_device_ws(*args, aligned, workspace.numel() - (aligned - base),
+                                                     s.cuda_stream), "tm_fke_advdiff_device_ws")
     return out.cpu().numpy() if as_numpy else out
 
 

@@ -25,6 +25,7 @@
 
 #include <cuda_runtime.h>
 
+#include <stdint.h>
 #include <vector>
 
 namespace {
@@ -119,41 +120,149 @@ __global__ void fke_cols_kernel(const T* AD, const T* AV, int L, const T* gDw, c
     }
 }
 
+// Workspace of one call (each region 256-byte aligned): w, A_D, A_V (T, L^2 each),
+// mux, muy (int, L^2 each), the wrapped stencils gDw, gVw (T, L each), smax (int).
+struct FkeLayout {
+    size_t w, AD, AV, mx, my, gD, gV, smax, end;
+};
+inline size_t al256(size_t v) { return (v + 255) / 256 * 256; }
+inline FkeLayout fke_layout(size_t esize, int L)
+{
+    const size_t n = (size_t)L * L;
+    FkeLayout y;
+    y.w = 0;
+    y.AD = al256(y.w + n * esize);
+    y.AV = al256(y.AD + n * esize);
+    y.mx = al256(y.AV + n * esize);
+    y.my = al256(y.mx + n * sizeof(int));
+    y.gD = al256(y.my + n * sizeof(int));
+    y.gV = al256(y.gD + (size_t)L * esize);
+    y.smax = al256(y.gV + (size_t)L * esize);
+    y.end = y.smax + 256;
+    return y;
+}
+
+// Stencils passed by value (the workspace entry point copies nothing from the host).
+struct FkeStencils {
+    double gD[TM_FKE_WS_MAX_RADIUS + 1];
+    double gV[TM_FKE_WS_MAX_RADIUS + 1];
+    int RD, RV;
+};
+
+// The stencils wrapped onto the lattice: residue i gets every g[|d|] with
+// d = i (mod L), |d| <= R, added in increasing d in FP64 and rounded once --
+// the same sums the host forms for the allocating entry point.
+template <typename T>
+__global__ void fke_wrap_kernel(const FkeStencils st, int L, T* gDw, T* gVw)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x) {
+        double sd = 0.0, sv = 0.0;
+        for (int d = -st.RD; d <= st.RD; ++d)
+            if (pmod(d, L) == i) sd += st.gD[d < 0 ? -d : d];
+        for (int d = -st.RV; d <= st.RV; ++d)
+            if (pmod(d, L) == i) sv += st.gV[d < 0 ? -d : d];
+        gDw[i] = (T)sd;
+        gVw[i] = (T)sv;
+    }
+}
+
+// The three passes on a caller-sized workspace whose wrapped stencils are already
+// set (or queued) on stream s; nothing is allocated and nothing waits.
+template <typename T>
+cudaError_t enqueue_passes(const void* rho, const void* gam, const void* vx, const void* vy, int L, double pref,
+                           double eps, int RD, int RV, void* out, unsigned char* ws, cudaStream_t s)
+{
+    const FkeLayout y = fke_layout(sizeof(T), L);
+    T* w = (T*)(ws + y.w);
+    T* AD = (T*)(ws + y.AD);
+    T* AV = (T*)(ws + y.AV);
+    int* mx = (int*)(ws + y.mx);
+    int* my = (int*)(ws + y.my);
+    const T* dgD = (const T*)(ws + y.gD);
+    const T* dgV = (const T*)(ws + y.gV);
+    int* smax = (int*)(ws + y.smax);
+    const size_t n = (size_t)L * L;
+    cudaError_t e = cudaMemsetAsync(smax, 0, sizeof(int), s);
+    if (e != cudaSuccess) return e;
+    const int grid = (int)((n + 255) / 256 < 8192 ? (n + 255) / 256 : 8192);
+    fke_prep_kernel<T><<<grid, 256, 0, s>>>((const T*)rho, (const T*)vx, (const T*)vy, L, (T)pref, (T)eps, w, mx, my,
+                                            smax);
+    fke_rows_kernel<T><<<grid, 256, 0, s>>>(w, (const T*)gam, mx, my, smax, L, dgD, dgV, RD, RV, AD, AV);
+    fke_cols_kernel<T><<<grid, 256, 0, s>>>(AD, AV, L, dgD, dgV, RD, RV, (T*)out);
+    return cudaGetLastError();
+}
+
 template <typename T>
 int run(const void* rho, const void* gam, const void* vx, const void* vy, int L, double pref, double eps,
         const double* gD, int RD, const double* gV, int RV, void* out, cudaStream_t s)
 {
-    const size_t n = (size_t)L * L;
     // the stencils wrapped onto the lattice: every image d = delta (mod L) of |d| <= R summed
     std::vector<double> wd(L, 0.0), wv(L, 0.0);
     for (int d = -RD; d <= RD; ++d) wd[((d % L) + L) % L] += gD[d < 0 ? -d : d];
     for (int d = -RV; d <= RV; ++d) wv[((d % L) + L) % L] += gV[d < 0 ? -d : d];
     std::vector<T> hd(wd.begin(), wd.end()), hv(wv.begin(), wv.end());
-    T *w = nullptr, *AD = nullptr, *AV = nullptr, *dgD = nullptr, *dgV = nullptr;
-    int *mx = nullptr, *my = nullptr, *smax = nullptr;
+    const FkeLayout y = fke_layout(sizeof(T), L);
+    unsigned char* ws = nullptr;
     int rc = TM_OK;
-    if (cudaMalloc(&w, n * sizeof(T)) != cudaSuccess || cudaMalloc(&AD, n * sizeof(T)) != cudaSuccess ||
-        cudaMalloc(&AV, n * sizeof(T)) != cudaSuccess || cudaMalloc(&mx, n * sizeof(int)) != cudaSuccess ||
-        cudaMalloc(&my, n * sizeof(int)) != cudaSuccess || cudaMalloc(&smax, sizeof(int)) != cudaSuccess ||
-        cudaMalloc(&dgD, L * sizeof(T)) != cudaSuccess || cudaMalloc(&dgV, L * sizeof(T)) != cudaSuccess) {
+    if (cudaMalloc(&ws, y.end) != cudaSuccess) {
         rc = TM_ERR_NOMEM;
-    } else {
-        cudaMemsetAsync(smax, 0, sizeof(int), s);
-        cudaMemcpyAsync(dgD, hd.data(), L * sizeof(T), cudaMemcpyHostToDevice, s);
-        cudaMemcpyAsync(dgV, hv.data(), L * sizeof(T), cudaMemcpyHostToDevice, s);
-        const int grid = (int)((n + 255) / 256 < 8192 ? (n + 255) / 256 : 8192);
-        fke_prep_kernel<T><<<grid, 256, 0, s>>>((const T*)rho, (const T*)vx, (const T*)vy, L, (T)pref, (T)eps, w, mx, my,
-                                                smax);
-        fke_rows_kernel<T><<<grid, 256, 0, s>>>(w, (const T*)gam, mx, my, smax, L, dgD, dgV, RD, RV, AD, AV);
-        fke_cols_kernel<T><<<grid, 256, 0, s>>>(AD, AV, L, dgD, dgV, RD, RV, (T*)out);
-        if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) rc = TM_ERR_CUDA;
+    } else if (cudaMemcpyAsync(ws + y.gD, hd.data(), L * sizeof(T), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+               cudaMemcpyAsync(ws + y.gV, hv.data(), L * sizeof(T), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+               enqueue_passes<T>(rho, gam, vx, vy, L, pref, eps, RD, RV, out, ws, s) != cudaSuccess ||
+               cudaStreamSynchronize(s) != cudaSuccess) {
+        rc = TM_ERR_CUDA;
     }
-    cudaFree(w); cudaFree(AD); cudaFree(AV); cudaFree(mx); cudaFree(my); cudaFree(smax); cudaFree(dgD); cudaFree(dgV);
+    cudaFree(ws);
     (void)cudaGetLastError();
     return rc;
 }
 
+template <typename T>
+int run_ws(const void* rho, const void* gam, const void* vx, const void* vy, int L, double pref, double eps,
+           const double* gD, int RD, const double* gV, int RV, void* out, void* ws, cudaStream_t s)
+{
+    FkeStencils st;
+    for (int d = 0; d <= TM_FKE_WS_MAX_RADIUS; ++d) {
+        st.gD[d] = d <= RD ? gD[d] : 0.0;
+        st.gV[d] = d <= RV ? gV[d] : 0.0;
+    }
+    st.RD = RD;
+    st.RV = RV;
+    const FkeLayout y = fke_layout(sizeof(T), L);
+    unsigned char* b = (unsigned char*)ws;
+    fke_wrap_kernel<T><<<(L + 255) / 256, 256, 0, s>>>(st, L, (T*)(b + y.gD), (T*)(b + y.gV));
+    if (enqueue_passes<T>(rho, gam, vx, vy, L, pref, eps, RD, RV, out, b, s) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return TM_ERR_CUDA;
+    }
+    return TM_OK;
+}
+
 }  // namespace
+
+extern "C" size_t tm_fke_workspace_bytes(int precision, int L)
+{
+    if ((precision != TM_FP64 && precision != TM_FP32) || L < 1 || L > 46340) return 0;
+    return fke_layout(precision == TM_FP64 ? 8 : 4, L).end;
+}
+
+extern "C" int tm_fke_advdiff_device_ws(const void* dev_rho, const void* dev_gamma, const void* dev_vx,
+                                        const void* dev_vy, int precision, int L, double pref, double eps,
+                                        const double* gD, int RD, const double* gV, int RV, void* dev_out,
+                                        void* dev_workspace, size_t workspace_bytes, void* stream)
+{
+    if (!dev_rho || !dev_gamma || !dev_vx || !dev_vy || !dev_out || !dev_workspace || !gD || !gV || L < 1 ||
+        L > 46340 || RD < 0 || RV < 0 || RD > TM_FKE_WS_MAX_RADIUS || RV > TM_FKE_WS_MAX_RADIUS ||
+        ((uintptr_t)dev_workspace & 255u) != 0)
+        return TM_ERR_INVALID;
+    const size_t need = tm_fke_workspace_bytes(precision, L);
+    if (need == 0 || workspace_bytes < need) return TM_ERR_INVALID;
+    if (precision == TM_FP64)
+        return run_ws<double>(dev_rho, dev_gamma, dev_vx, dev_vy, L, pref, eps, gD, RD, gV, RV, dev_out, dev_workspace,
+                              (cudaStream_t)stream);
+    return run_ws<float>(dev_rho, dev_gamma, dev_vx, dev_vy, L, pref, eps, gD, RD, gV, RV, dev_out, dev_workspace,
+                         (cudaStream_t)stream);
+}
 
 extern "C" int tm_fke_advdiff_device(const void* dev_rho, const void* dev_gamma, const void* dev_vx,
                                      const void* dev_vy, int precision, int L, double pref, double eps,
