@@ -187,6 +187,17 @@ int tm_batch_set_launch(tm_batch* b, int rows_per_task, int ctas_per_sm);
 int tm_batch_get_launch(const tm_batch* b, int* rows_per_task, int* ctas_per_sm);
 int tm_batch_autotune(tm_batch* b, int steps_per_trial);
 
+/* Spreading runs (DP, stochastic): spreading_exp_Dornic_2D
+ * (stochasticSPDP.cpp:1145-1298) started from a single seed.  With enable = 1,
+ * every measurement also gives f2 = the sum over occupied sites (rho > 0) of the
+ * squared distance (row - cy)^2 + (col - cx)^2 from the seed site
+ * (meansq_spread_of_vector, :156-170; cx, cy = -1: L/2, the reference's seed),
+ * so tm_batch_obs_width becomes 3; and an instance whose border row or column
+ * holds an occupied site stops before its next measurement or step, as the
+ * reference's theborderwall check ends the replicate (:380-390, 1206-1213): its
+ * later measurements are 0 and it downloads as zeros, like an extinct one. */
+int tm_batch_set_spreading(tm_batch* b, int enable, int cx, int cy);
+
 /* Per-site loss coefficient b_v for a DP batch (host, packed like the state):
  * the remainder uses b_v[i] in place of tm_dp_model.b -- the termite-mound
  * field of sde_RFT_2D_improved_Euler_w_mounds_RT_RK4_SNAPSHOTS_DEF.f:196-428,

@@ -112,3 +112,37 @@ def test_invalid_arguments_are_rejected_without_gpu(tmlib):
     }
     for name, args in calls.items():
         assert getattr(L, name)(*args) == bad, name
+
+
+def test_lnspace_matches_reference():
+    """api.lnspace equals the reference's lnspace<int> (the stationary finite-size
+    sweep's lattice sides) double for double."""
+    import os
+    from trophic_maelstorm_gb300 import api
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_lnspace.npz"))
+    for k, (a, b, n) in enumerate(g["cases"]):
+        want = g[f"lnspace_{k}"]
+        got = np.array(api.lnspace(int(a), int(b), int(n)))
+        assert np.array_equal(got, want), (a, b, n)
+        assert [int(x) for x in got] == [int(x) for x in want]
+
+
+def test_stationary_windows_follow_reference():
+    from trophic_maelstorm_gb300 import api
+    assert api.stationary_window(31) == (300.0, 900.0) and api.stationary_window(50) == (300.0, 900.0)
+    assert api.stationary_window(51) == (1000.0, 2500.0) and api.stationary_window(100) == (1000.0, 2500.0)
+    assert api.stationary_window(101) == (1250.0, 8000.0) and api.stationary_window(150) == (1250.0, 8000.0)
+    assert api.stationary_window(151) == (1400.0, 10000.0) and api.stationary_window(200) == (1400.0, 10000.0)
+    assert api.stationary_window(201) == (2000.0, 15000.0)
+    with pytest.raises(ValueError):
+        api.stationary_window(30)
+
+
+def test_spreading_rows_average_over_running_replicates():
+    from trophic_maelstorm_gb300 import api
+    n = np.array([[1, 4, 0], [1, 2, 6]], float)       # replicate 0 stops after t1
+    sq = np.array([[0, 8, 0], [0, 2, 30]], float)
+    rows = api.spreading_rows(3, 0.7, [0.0, 0.1, 0.2], n, sq)
+    assert rows[0].tolist() == [3.0, 0.7, 0.0, 1.0, 0.0, 2.0]
+    assert rows[1].tolist() == [3.0, 0.7, 0.1, 3.0, 1.5, 2.0]
+    assert rows[2].tolist() == [3.0, 0.7, 0.2, 6.0, 5.0, 1.0]

@@ -33,7 +33,7 @@ EXPORTS = (
     "tm_batch_set_site_coeff", "tm_batch_box_means", "tm_fke_advdiff_device",
     "tm_mlp_create", "tm_mlp_destroy", "tm_mlp_set_params", "tm_mlp_get_params", "tm_mlp_set_data",
     "tm_mlp_loss_grad", "tm_mlp_train", "tm_mlp_predict", "tm_set_test_probe",
-    "tm_fke_workspace_bytes", "tm_fke_advdiff_device_ws",
+    "tm_fke_workspace_bytes", "tm_fke_advdiff_device_ws", "tm_batch_set_spreading",
 )
 
 
@@ -124,6 +124,7 @@ def lib():
             "tm_mlp_train": ([vp, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, dp], C.c_int),
             "tm_mlp_predict": ([vp, fp, C.c_int, fp], C.c_int),
             "tm_set_test_probe": ([vp, C.c_uint32], C.c_int),
+            "tm_batch_set_spreading": ([vp, C.c_int, C.c_int, C.c_int], C.c_int),
             "tm_fke_workspace_bytes": ([C.c_int, C.c_int], C.c_size_t),
             "tm_fke_advdiff_device_ws": ([vp, vp, vp, vp, C.c_int, C.c_int, C.c_double, C.c_double, dp, C.c_int, dp,
                                           C.c_int, vp, vp, C.c_size_t, vp], C.c_int),

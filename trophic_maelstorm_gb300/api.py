@@ -35,6 +35,19 @@ def linspace(start, end, num):
     return [float(start) + delta * i for i in range(num - 1)] + [float(end)]
 
 
+def lnspace(start, end, num):
+    """Natural-log-spaced points as the reference writes them (stochasticSPDP.cpp:281-301):
+    e^(log start + i delta) for i < num - 1, then end exactly."""
+    if num == 0:
+        return []
+    if num == 1:
+        return [float(start)]
+    lo, hi = math.log(float(start)), math.log(float(end))
+    delta = (hi - lo) / (num - 1)
+    base = math.exp(1)
+    return [math.pow(base, lo + delta * i) for i in range(num - 1)] + [float(end)]
+
+
 def logarithm10_time_bins(t_max: float, dt: float) -> list[float]:
     """Measurement times 10^0 .. 10^floor1(log10 t_max), 25 per decade, snapped
     down to the dt grid and de-duplicated (stochasticSPDP.cpp:336-378)."""
@@ -240,6 +253,13 @@ class Batch:
     def autotune(self, steps_per_trial=4):
         T.check(T.lib().tm_batch_autotune(self._h, steps_per_trial), "tm_batch_autotune")
         return self.get_launch()
+
+    def set_spreading(self, enable=True, cx=-1, cy=-1):
+        """Spreading runs: measurements add the summed squared distance of occupied
+        sites from the seed (obs width 3), and instances stop once activity reaches
+        the lattice's edge (tm_batch_set_spreading)."""
+        T.check(T.lib().tm_batch_set_spreading(self._h, int(enable), int(cx), int(cy)), "tm_batch_set_spreading")
+        self.obs_width = T.lib().tm_batch_obs_width(self._h)
 
     def set_site_coeff(self, coeff):
         """Per-site loss coefficient b_v (list of (L, L) arrays or a packed buffer; None: uniform b)."""
@@ -516,3 +536,138 @@ def critical_exp_delta(Rho_0, div, t_max, a_start, a_end, b, D, sigma, dt, dx, r
         return None, None
     return (np.concatenate([merged[ia][0] for ia in range(div)]),
             np.concatenate([merged[ia][1] for ia in range(div)]))
+
+# ------------------------------------------------------ finite-size and spreading sweeps
+def init_fullframe(g):
+    """Every site at 1 (init_fullframe, stochasticSPDP.cpp:39-44)."""
+    return np.ones(g * g)
+
+
+def init_solitarytear(g):
+    """A single occupied site at (int(g/2), int(g/2)) (init_solitarytear, stochasticSPDP.cpp:88-95)."""
+    a = np.zeros(g * g)
+    h = int(g / 2.0)
+    a[g * h + h] = 1.0
+    return a
+
+
+def _ragged_dp_rows(ctx, groups, t_meas, t_max, a, b, D, sigma, dt, dx, r, seed, precision):
+    """One batch for several lattice sizes: groups = [(L, init frame)], r replicates each,
+    measured on one grid; returns [(L, rows, status)] in group order.  Replicate j of
+    group i has the Philox key seed + i r + j."""
+    steps, times, n_early = reference_step_grid(t_meas, dt)
+    Ls, seeds = [], []
+    for i, (L, _) in enumerate(groups):
+        for j in range(r):
+            Ls.append(L); seeds.append(seed + i * r + j)
+    inst = instances(Ls, seeds, a)
+    model = dp_model(b=b, D=D, sigma=sigma, dt=dt, dx=dx)
+    dtype = np.float64 if precision == T.TM_FP64 else np.float32
+    init = pack([np.asarray(f, np.float64).reshape(L, L) for L, f in groups for _ in range(r)], inst, 1, dtype)
+    obs, st, _ = run_dp(ctx, model, inst, init, max(steps), steps, precision)
+    out = []
+    for i, (L, _) in enumerate(groups):
+        sl = slice(i * r, (i + 1) * r)
+        out.append((L, replicate_rows(a, L, times, n_early, obs[:, sl, 0].T, obs[:, sl, 1].T), st[sl]))
+    return out
+
+
+def critical_exp_finite_scaling_collapse(div, g_st, g_end, t_max, a_c, b, D, sigma, dt, dx, r, *, seed=0,
+                                         precision=T.TM_FP64, ctx: Context | None = None):
+    """The finite-size sweep of stochasticSPDP.cpp:1424-1536 at a_c: lattice sides
+    int(linspace(g_st, g_end, div)), r replicates each from a full frame, measured on
+    logarithm10_time_bins(t_max, dt); every side in one ragged batch.  Returns the
+    reference's rows {a, L, t, <<rho>_x>_r, Var, #surviving, #active, surv-alt} in
+    side order, and the replicates' status bits."""
+    ctx = ctx or Context(0)
+    g_space = [int(g) for g in linspace(g_st, g_end, div)]
+    res = _ragged_dp_rows(ctx, [(g, init_fullframe(g)) for g in g_space], logarithm10_time_bins(t_max, dt), t_max,
+                          a_c, b, D, sigma, dt, dx, r, seed, precision)
+    return np.concatenate([rows for _, rows, _ in res]), np.concatenate([st for _, _, st in res])
+
+
+def stationary_window(g):
+    """Measurement window (t_start, t_end) of the stationary finite-size sweep for side g
+    (stochasticSPDP.cpp:1600-1610).  The reference sets none for g <= 30 (its values are
+    then uninitialised), so such sides are rejected."""
+    if 30 < g <= 50:
+        return 300.0, 900.0
+    if 50 < g <= 100:
+        return 1000.0, 2500.0
+    if 100 < g <= 150:
+        return 1250.0, 8000.0
+    if 150 < g <= 200:
+        return 1400.0, 10000.0
+    if g > 200:
+        return 2000.0, 15000.0
+    raise ValueError(f"critical_exp_finite_scaling_stationary: no measurement window for L = {g} <= 30")
+
+
+def critical_exp_finite_scaling_stationary(div, g_st, g_end, t_lim, t_max, a_c, b, D, sigma, dt, dx, r, *, seed=0,
+                                           precision=T.TM_FP64, ctx: Context | None = None):
+    """The stationary finite-size sweep of stochasticSPDP.cpp:1539-1670 at a_c: sides
+    int(lnspace(g_st, g_end, div)), r replicates each from a full frame, each side
+    measured at linspace(t_start, t_end, 30) of its window (stationary_window).
+    Sides sharing a window run as one ragged batch.  t_lim and t_max are accepted
+    for the reference's argument order; the reference's runs end at t_end + 10,
+    after their last measurement, so they do not change the rows.  Returns rows in
+    side order and the replicates' status bits."""
+    ctx = ctx or Context(0)
+    g_space = [int(g) for g in lnspace(g_st, g_end, div)]
+    windows = [stationary_window(g) for g in g_space]
+    by_window = {}
+    for i, (g, w) in enumerate(zip(g_space, windows)):
+        by_window.setdefault(w, []).append(i)
+    per_side = {}
+    for w, idx in by_window.items():
+        t_meas = linspace(w[0], w[1], 30)
+        res = _ragged_dp_rows(ctx, [(g_space[i], init_fullframe(g_space[i])) for i in idx], t_meas, w[1] + 10,
+                              a_c, b, D, sigma, dt, dx, r, seed + 7919 * min(idx), precision)
+        for i, (_, rows, st) in zip(idx, res):
+            per_side[i] = (rows, st)
+    return (np.concatenate([per_side[i][0] for i in range(len(g_space))]),
+            np.concatenate([per_side[i][1] for i in range(len(g_space))]))
+
+
+def spreading_rows(block, a, times, n_active, sq_dist):
+    """Rows {block, a, t, <N(t)>_r, <MSD(t)>_r, #surviving} of spreading runs from
+    per-replicate series n_active[j, i] (occupied sites) and sq_dist[j, i] (summed
+    squared distance): means over the replicates still running at t
+    (spreading_incremental_surv_runs, stochasticSPDP.cpp:230-252; the reference's
+    first column is the OpenMP thread, here the block index)."""
+    rows = []
+    for i, t in enumerate(times):
+        alive = n_active[:, i] > 0
+        ns = int(alive.sum())
+        N = float(n_active[alive, i].mean()) if ns else 0.0
+        msd = float((sq_dist[alive, i] / n_active[alive, i]).mean()) if ns else 0.0
+        rows.append([float(block), a, float(t), N, msd, float(ns)])
+    return np.array(rows)
+
+
+def critical_exp_theta_delta(Rho_0, div, t_max, a_c, b, D, sigma, dt, dx, r, g, *, seed=0, precision=T.TM_FP64,
+                             ctx: Context | None = None):
+    """Spreading experiments of stochasticSPDP.cpp:1673-1764: div blocks of r
+    replicates started from a single seed at the centre (init_solitarytear; Rho_0 is
+    ignored, as in the reference, which overwrites it), each measuring the number of
+    occupied sites N(t) and their mean squared distance from the seed on
+    logarithm10_time_bins(t_max, dt), and stopping once activity reaches the edge
+    (spreading_exp_Dornic_2D, :1145-1298).  All div x r replicates run as one batch.
+    Returns rows {block, a, t, <N>_r, <MSD>_r, #surviving} in block order, and the
+    replicates' status bits."""
+    ctx = ctx or Context(0)
+    t_meas = logarithm10_time_bins(t_max, dt)
+    steps, times, _ = reference_step_grid(t_meas, dt)
+    n = div * r
+    inst = instances([g] * n, [seed + j for j in range(n)], a_c)
+    dtype = np.float64 if precision == T.TM_FP64 else np.float32
+    bt = Batch(ctx, dp_model(b=b, D=D, sigma=sigma, dt=dt, dx=dx), inst, precision)
+    try:
+        bt.set_spreading(True)
+        bt.upload([init_solitarytear(g).reshape(g, g).astype(dtype)] * n)
+        obs, st = bt.advance(max(steps), steps)
+    finally:
+        bt.close()
+    rows = [spreading_rows(i, a_c, times, obs[:, i * r:(i + 1) * r, 1].T, obs[:, i * r:(i + 1) * r, 2].T)
+            for i in range(div)]
+    return np.concatenate(rows), st

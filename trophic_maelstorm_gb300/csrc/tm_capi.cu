@@ -83,6 +83,8 @@ struct tm_batch {
     bool ramped = false;
 
     unsigned probe = 0;         // TM_PROBE_* flags of the context when the batch was created
+    int spreading = 0;          // DP spreading runs: squared-distance measurement, border stop
+    int spread_cx = -1, spread_cy = -1;
     int rows_per_task = 8;
     int ctas_per_sm = 4;
     int4* d_tasks = nullptr;
@@ -106,6 +108,8 @@ struct tm_batch {
 };
 
 namespace {
+
+int obs_w(const tm_batch* b) { return b->model == 0 ? (b->spreading ? 3 : 2) : 4; }
 
 void free_graphs(tm_batch* b)
 {
@@ -253,7 +257,9 @@ cudaError_t enqueue_step_t(tm_batch* b, int src_idx, const long long* step_base,
             if (e != cudaSuccess) return e;
         }
         DornicArgs<T> a = dornic_args<T>(b, in, out, step_base, step_off);
-        return launch_dornic<T>(a, m.remainder == TM_REM_RK4 ? 1 : 0, warp_grid(b, b->n_tasks), 256, s);
+        e = launch_dornic<T>(a, m.remainder == TM_REM_RK4 ? 1 : 0, warp_grid(b, b->n_tasks), 256, s);
+        if (e == cudaSuccess && b->spreading) e = launch_border_stop<T>(out, b->tables(), b->n_inst, s);
+        return e;
     }
     const tm_rietkerk_model& m = b->rkm;
     const int grid_rk = std::max(1, std::min(b->n_btasks, b->ctx->num_sms * RK_CTAS));
@@ -320,19 +326,19 @@ int run_steps(tm_batch* b, int64_t n)
 int measure_into(tm_batch* b, int j)
 {
     cudaStream_t s = b->ctx->stream;
-    const int W = b->model == 0 ? 2 : 4;
+    const int W = obs_w(b);
     InstTables it = b->tables();
     if (b->model == 1) it.alive = nullptr;
     const int grid = warp_grid(b, b->n_tasks);
     cudaError_t e;
     if (b->precision == TM_FP64)
         e = launch_measure<double>((const double*)b->buf[b->cur], it, b->d_tasks, b->n_tasks, b->nf, b->d_partial,
-                                   grid, 256, s);
+                                   grid, 256, s, b->spreading, b->spread_cx, b->spread_cy);
     else
         e = launch_measure<float>((const float*)b->buf[b->cur], it, b->d_tasks, b->n_tasks, b->nf, b->d_partial, grid,
-                                  256, s);
+                                  256, s, b->spreading, b->spread_cx, b->spread_cy);
     TM_CUDA(e);
-    TM_CUDA(launch_finalize(b->d_partial, b->d_task_begin, it, b->n_inst, b->nf, b->model == 0,
+    TM_CUDA(launch_finalize(b->d_partial, b->d_task_begin, it, b->n_inst, b->nf, b->model == 0, b->spreading,
                             b->d_obs + (size_t)j * b->n_inst * W, s));
     return TM_OK;
 }
@@ -387,7 +393,7 @@ int batch_common_init(tm_batch* b, const tm_instance* inst, int n)
 int obs_reserve(tm_batch* b, int n_meas)
 {
     if (n_meas <= b->obs_cap) return TM_OK;
-    const int W = b->model == 0 ? 2 : 4;
+    const int W = obs_w(b);
     cudaFree(b->d_obs);
     b->d_obs = nullptr;
     TM_CUDA(dalloc(&b->d_obs, (size_t)n_meas * b->n_inst * W));
@@ -577,7 +583,7 @@ int64_t tm_batch_total_elems(const tm_batch* b) { return b ? b->total : -1; }
 int64_t tm_batch_instance_offset(const tm_batch* b, int k) { return (b && k >= 0 && k < b->n_inst) ? b->off[k] : -1; }
 int64_t tm_batch_field_stride(const tm_batch* b, int k) { return (b && k >= 0 && k < b->n_inst) ? b->fstride[k] : -1; }
 int tm_batch_num_fields(const tm_batch* b) { return b ? b->nf : -1; }
-int tm_batch_obs_width(const tm_batch* b) { return b ? (b->model == 0 ? 2 : 4) : -1; }
+int tm_batch_obs_width(const tm_batch* b) { return b ? obs_w(b) : -1; }
 int64_t tm_batch_step(const tm_batch* b) { return b ? b->step : -1; }
 
 // After an upload: step counter, extinction flags, and the status bits of the
@@ -684,6 +690,14 @@ int tm_batch_advance(tm_batch* b, int64_t n_steps, const int64_t* meas, int n_me
     TM_CUDA(cudaSetDevice(b->ctx->device));
     int rc = obs_reserve(b, n_meas);
     if (rc) return rc;
+    if (b->spreading) {  // the border check of the state about to be measured and stepped
+        cudaError_t e = b->precision == TM_FP64
+                            ? launch_border_stop<double>((const double*)b->buf[b->cur], b->tables(), b->n_inst,
+                                                         b->ctx->stream)
+                            : launch_border_stop<float>((const float*)b->buf[b->cur], b->tables(), b->n_inst,
+                                                        b->ctx->stream);
+        TM_CUDA(e);
+    }
     int j = 0;
     while (true) {
         while (j < n_meas && meas[j] == b->step) {
@@ -696,7 +710,7 @@ int tm_batch_advance(tm_batch* b, int64_t n_steps, const int64_t* meas, int n_me
         rc = run_steps(b, target - b->step);
         if (rc) return rc;
     }
-    const int W = b->model == 0 ? 2 : 4;
+    const int W = obs_w(b);
     if (n_meas > 0)
         TM_CUDA(cudaMemcpyAsync(obs, b->d_obs, (size_t)n_meas * b->n_inst * W * sizeof(double),
                                 cudaMemcpyDeviceToHost, b->ctx->stream));
@@ -796,6 +810,23 @@ int tm_batch_autotune(tm_batch* b, int steps_per_trial)
     cudaFree(save);
     if (rc) return rc;
     return tm_batch_set_launch(b, best_r, best_c);
+}
+
+int tm_batch_set_spreading(tm_batch* b, int enable, int cx, int cy)
+{
+    if (!b || b->model != 0 || b->dpm.deterministic || cx < -1 || cy < -1) return TM_ERR_INVALID;
+    for (int k = 0; k < b->n_inst; ++k)
+        if (cx >= b->inst[k].L || cy >= b->inst[k].L) return TM_ERR_INVALID;
+    TM_CUDA(cudaSetDevice(b->ctx->device));
+    TM_CUDA(cudaStreamSynchronize(b->ctx->stream));
+    b->spreading = enable ? 1 : 0;
+    b->spread_cx = cx;
+    b->spread_cy = cy;
+    free_graphs(b);
+    cudaFree(b->d_obs);   // the measurement width changed
+    b->d_obs = nullptr;
+    b->obs_cap = 0;
+    return TM_OK;
 }
 
 int tm_batch_set_site_coeff(tm_batch* b, const void* host_coeff)

@@ -81,12 +81,15 @@ template <typename T>
 cudaError_t launch_rk4(const RK4Args<T>& a, bool det, int grid, cudaStream_t s);
 template <typename T>
 cudaError_t launch_measure(const T* state, const InstTables& it, const int4* tasks, int n_tasks, int nf,
-                           double* partial, int grid, int block, cudaStream_t s);
+                           double* partial, int grid, int block, cudaStream_t s, int spread = 0, int cx = -1,
+                           int cy = -1);
+template <typename T>
+cudaError_t launch_border_stop(const T* state, const InstTables& it, int n_inst, cudaStream_t s);
 template <typename T>
 cudaError_t launch_validate(const T* state, const InstTables& it, const int4* tasks, int n_tasks, int nf, int grid,
                             cudaStream_t s);
 cudaError_t launch_finalize(const double* partial, const int* task_begin, const InstTables& it, int n_inst, int nf,
-                            int dp_extinction, double* obs_row, cudaStream_t s);
+                            int dp_extinction, int spread, double* obs_row, cudaStream_t s);
 cudaError_t launch_consts(const double* a0, const double* astep, int n, double diff4, double sigma2, double dt,
                           const long long* step_base, long long step_off, Dc4* out, cudaStream_t s);
 cudaError_t launch_set_step(long long* d_step, long long v, cudaStream_t s);

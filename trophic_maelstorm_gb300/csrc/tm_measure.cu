@@ -61,10 +61,14 @@ struct ColSum<float> {
     }
 };
 
-// partial[t*4 + f]: f = 0..nf-1 field sums, 3 = sites with field 0 > 0
+// partial[t*4 + f]: f = 0..nf-1 field sums, 3 = sites with field 0 > 0.  With
+// spread (DP), f = 1 is the sum over occupied sites of the squared distance
+// (row - cy)^2 + (col - cx)^2 from the seed site (meansq_spread_of_vector,
+// stochasticSPDP.cpp:156-170), summed as integers; cx, cy < 0 mean L/2.
 template <typename T>
 __global__ void __launch_bounds__(256) measure_kernel(const T* state, const InstTables it, const int4* tasks,
-                                                      int n_tasks, int nf, double* partial)
+                                                      int n_tasks, int nf, double* partial, int spread, int scx,
+                                                      int scy)
 {
     const int lane = threadIdx.x & 31;
     const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
@@ -76,16 +80,22 @@ __global__ void __launch_bounds__(256) measure_kernel(const T* state, const Inst
         const int x = tk.y + lane;
         ColSum<T> c0, c1, c2;
         int ac = 0;
+        long long sq = 0;
         const bool on = it.alive == nullptr || it.alive[k] != 0;   // warp-uniform
         if (on) {
             const T* base = state + it.off[k];
             const long long fs = it.fstride[k];
             const bool in = x < L;
+            const long long cx = scx < 0 ? L / 2 : scx, cy = scy < 0 ? L / 2 : scy;
             for (int r = 0; r < tk.w; ++r) {
                 const long long i = (long long)(tk.z + r) * L + x;
                 const T v = in ? base[i] : T(0);
                 c0.add(v);
                 ac += __popc(__ballot_sync(0xffffffffu, v > T(0)));
+                if (spread && v > T(0)) {
+                    const long long dy = (long long)(tk.z + r) - cy, dx = (long long)x - cx;
+                    sq += dy * dy + dx * dx;
+                }
                 if (nf == 3 && in) {
                     c1.add(base[i + fs]);
                     c2.add(base[i + 2 * fs]);
@@ -95,6 +105,7 @@ __global__ void __launch_bounds__(256) measure_kernel(const T* state, const Inst
         const double s0 = c0.warp_total();
         double s1 = 0.0, s2 = 0.0;
         if (nf == 3) { s1 = c1.warp_total(); s2 = c2.warp_total(); }
+        if (spread) s1 = warp_sum((double)sq);   // integers below 2^53: exact in any order
         if (lane == 0) {
             partial[4LL * t + 0] = s0;
             partial[4LL * t + 1] = s1;
@@ -106,16 +117,45 @@ __global__ void __launch_bounds__(256) measure_kernel(const T* state, const Inst
 
 template <typename T>
 cudaError_t launch_measure(const T* state, const InstTables& it, const int4* tasks, int n_tasks, int nf,
-                           double* partial, int grid, int block, cudaStream_t s)
+                           double* partial, int grid, int block, cudaStream_t s, int spread, int cx, int cy)
 {
     if (n_tasks <= 0) return cudaSuccess;
-    measure_kernel<T><<<grid, block, 0, s>>>(state, it, tasks, n_tasks, nf, partial);
+    measure_kernel<T><<<grid, block, 0, s>>>(state, it, tasks, n_tasks, nf, partial, spread, cx, cy);
     return cudaGetLastError();
 }
 template cudaError_t launch_measure<float>(const float*, const InstTables&, const int4*, int, int, double*, int, int,
-                                           cudaStream_t);
+                                           cudaStream_t, int, int, int);
 template cudaError_t launch_measure<double>(const double*, const InstTables&, const int4*, int, int, double*, int,
-                                            int, cudaStream_t);
+                                            int, cudaStream_t, int, int, int);
+
+// Spreading runs stop once activity reaches the lattice's edge (theborderwall,
+// stochasticSPDP.cpp:380-390, checked before every step at :1206-1213): one warp
+// per live instance scans its four border rows/columns and marks it stopped
+// (alive = 0, so later steps skip it and its later measurements are 0).
+template <typename T>
+__global__ void border_stop_kernel(const T* state, const InstTables it, int n_inst)
+{
+    const int lane = threadIdx.x & 31;
+    const int k = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (k >= n_inst || it.alive[k] == 0) return;
+    const int L = it.L[k];
+    const T* base = state + it.off[k];
+    bool hit = false;
+    for (int i = lane; i < L; i += 32)
+        hit = hit || base[i] > T(0) || base[(long long)i * L] > T(0) || base[(long long)(L - 1) * L + i] > T(0) ||
+              base[(long long)i * L + L - 1] > T(0);
+    if (__any_sync(0xffffffffu, hit) && lane == 0) it.alive[k] = 0;
+}
+
+template <typename T>
+cudaError_t launch_border_stop(const T* state, const InstTables& it, int n_inst, cudaStream_t s)
+{
+    if (n_inst <= 0) return cudaSuccess;
+    border_stop_kernel<T><<<(n_inst * 32 + 255) / 256, 256, 0, s>>>(state, it, n_inst);
+    return cudaGetLastError();
+}
+template cudaError_t launch_border_stop<float>(const float*, const InstTables&, int, cudaStream_t);
+template cudaError_t launch_border_stop<double>(const double*, const InstTables&, int, cudaStream_t);
 
 // Status bits of an uploaded state, per instance: TM_STATUS_NAN_BIT for a NaN or
 // Inf and TM_STATUS_NEG_BIT for a negative value in any field -- the checks the
@@ -157,11 +197,12 @@ template cudaError_t launch_validate<float>(const float*, const InstTables&, con
 template cudaError_t launch_validate<double>(const double*, const InstTables&, const int4*, int, int, int,
                                              cudaStream_t);
 
-// One warp per instance: obs_row[k*W + f], W = 2 (DP: mean, active) or 4
-// (Rietkerk: mean P, W, O, active P).  With dp_extinction, an instance seen with
-// no active site is marked extinct (stochasticSPDP.cpp:1021-1022).
+// One warp per instance: obs_row[k*W + f], W = 2 (DP: mean, active), 3 (DP
+// spreading: mean, active, summed squared distance) or 4 (Rietkerk: mean P, W, O,
+// active P).  With dp_extinction, an instance seen with no active site is marked
+// extinct (stochasticSPDP.cpp:1021-1022).
 __global__ void finalize_kernel(const double* partial, const int* task_begin, const InstTables it, int n_inst, int nf,
-                                int dp_extinction, double* obs_row)
+                                int dp_extinction, int spread, double* obs_row)
 {
     const int lane = threadIdx.x & 31;
     const int k = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
@@ -178,7 +219,11 @@ __global__ void finalize_kernel(const double* partial, const int* task_begin, co
     if (lane == 0) {
         const bool dead = it.alive != nullptr && it.alive[k] == 0;
         const double n = (double)it.L[k] * (double)it.L[k];
-        if (nf == 1) {
+        if (nf == 1 && spread) {
+            obs_row[3LL * k + 0] = dead ? 0.0 : s0 / n;
+            obs_row[3LL * k + 1] = dead ? 0.0 : ac;
+            obs_row[3LL * k + 2] = dead ? 0.0 : s1;
+        } else if (nf == 1) {
             obs_row[2LL * k + 0] = dead ? 0.0 : s0 / n;
             obs_row[2LL * k + 1] = dead ? 0.0 : ac;
         } else {
@@ -192,12 +237,12 @@ __global__ void finalize_kernel(const double* partial, const int* task_begin, co
 }
 
 cudaError_t launch_finalize(const double* partial, const int* task_begin, const InstTables& it, int n_inst, int nf,
-                            int dp_extinction, double* obs_row, cudaStream_t s)
+                            int dp_extinction, int spread, double* obs_row, cudaStream_t s)
 {
     if (n_inst <= 0) return cudaSuccess;
     const int threads = 256;
     const int grid = (n_inst * 32 + threads - 1) / threads;
-    finalize_kernel<<<grid, threads, 0, s>>>(partial, task_begin, it, n_inst, nf, dp_extinction, obs_row);
+    finalize_kernel<<<grid, threads, 0, s>>>(partial, task_begin, it, n_inst, nf, dp_extinction, spread, obs_row);
     return cudaGetLastError();
 }
 
