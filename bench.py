@@ -56,16 +56,12 @@ def a_values():
 
 def workload(kind="sweep"):
     Ls, seeds, avs = [], [], []
-    k = 0
     if kind == "l1024x64":  # profiling case: 64 instances of the L=1024 subset (268 MB per state buffer)
         for r in range(64):
             Ls.append(1024); seeds.append(1_000_003 * r + 17); avs.append(float(a_values()[r % NA]))
         return Ls, seeds, avs
-    for L in LS:
-        for a in a_values():
-            for r in range(REPS):
-                Ls.append(L); seeds.append(1_000_003 * k + 17); avs.append(float(a)); k += 1
-    return Ls, seeds, avs
+    from trophic_maelstorm_gb300.study import sweep_workload
+    return sweep_workload(LS, REPS, NA, A_CENTER)
 
 
 def init_field(L, rng):
@@ -160,31 +156,39 @@ def job_throughput(units_per_rank, seconds_per_rank, world):
 
 
 # ------------------------------------------------------------------ CPU baseline
-def cpu_run(n_inst_sample, steps, threads):
-    """The oracle (CPU restatement of the reference step) over a bounded sample of
-    L=1024 instances of the workload; returns site-updates/s."""
+def cpu_sample(dtype=np.float32):
+    """The bounded CPU sample of the sweep: one instance per (L, a) -- every lattice
+    side and a-value of the workload in its proportions, 1/32 of its replicates
+    (80 instances, 22.3 M sites per step) -- with the workload's keys and start."""
+    Ls, seeds, avs = workload("sweep")
+    pick = list(range(0, len(Ls), REPS))
+    rng = np.random.default_rng(0)
+    return ([Ls[i] for i in pick], [seeds[i] for i in pick], [avs[i] for i in pick],
+            [init_field(Ls[i], rng).astype(dtype) for i in pick])
+
+
+def cpu_run(steps, threads, dtype=np.float32):
+    """The oracle (CPU restatement of the reference step) over the sample, OpenMP
+    over instances; returns (site-updates/s, seconds)."""
     from oracle import oracle as o
     o.build()
-    rng = np.random.default_rng(0)
-    avs = a_values()
-    Ls = [1024] * n_inst_sample
-    params = [o.dp_params(a=float(avs[k % NA]), **MODEL) for k in range(n_inst_sample)]
-    fields = [init_field(1024, rng) for _ in range(n_inst_sample)]
+    Ls, seeds, avs, fields = cpu_sample(dtype)
+    params = [o.dp_params(a=a, **MODEL) for a in avs]
     t0 = time.perf_counter()
-    o.dp_batch_run_f32(params, Ls, list(range(n_inst_sample)), fields, steps, threads)
+    o.dp_batch_run(params, Ls, seeds, fields, steps, threads)
     el = time.perf_counter() - t0
-    return n_inst_sample * 1024 * 1024 * steps / el, el
+    return sum(L * L for L in Ls) * steps / el, el
 
 
 def cpu_baseline(threads, budget_s=15.0):
-    # calibrate on one step, then size the sample to about budget_s seconds
-    n_inst = max(threads, 8)
-    rate, el = cpu_run(n_inst, 1, threads)
-    steps = max(1, int(budget_s * rate / (n_inst * 1024 * 1024)))
-    rate, el = cpu_run(n_inst, steps, threads)
+    # calibrate on one step, then size the run to about budget_s seconds
+    rate, el = cpu_run(1, threads)
+    steps = max(1, int(budget_s / max(el, 1e-6)))
+    rate, el = cpu_run(steps, threads)
     return {"value": rate, "unit": "site-updates/s", "cores": threads, "kind": "port",
-            "sample": f"{n_inst} instances of the L=1024 subset x {steps} steps (fully active start), "
-                      f"{el:.1f} s, OpenMP over instances"}
+            "sample": f"one instance per (L, a) of the sweep (80 instances, every L in {{64..1024}}, "
+                      f"22.3 M sites) x {steps} steps from the fully active start, FP32 port, {el:.1f} s, "
+                      f"OpenMP over instances"}
 
 
 def workload_config(kind):
@@ -204,19 +208,20 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     from oracle import oracle as o
     o.build()
-    rng = np.random.default_rng(0)
-    avs = a_values()
-    n_inst = max(threads, 8)
-    params = [o.dp_params(a=float(avs[k % NA]), **MODEL) for k in range(n_inst)]
-    fields = [init_field(1024, rng) for _ in range(n_inst)]
-    seeds = list(range(n_inst))
-    for _ in range(args.warmup):
-        o.dp_batch_run_f32(params, [1024] * n_inst, seeds, fields, 1, threads)
+    Ls, seeds, avs, fields = cpu_sample(np.float32)
+    params = [o.dp_params(a=a, **MODEL) for a in avs]
+    sites = sum(L * L for L in Ls)
+    o.dp_batch_run(params, Ls, seeds, fields, args.warmup, threads)
     t0 = time.perf_counter()
-    o.dp_batch_run_f32(params, [1024] * n_inst, seeds, fields, args.steps, threads)
+    o.dp_batch_run(params, Ls, seeds, fields, args.steps, threads)
     el = time.perf_counter() - t0
-    sites = n_inst * 1024 * 1024
     val = sites * args.steps / el
+    # the reference computes in FP64: the FP64 port on the same sample, fewer steps
+    Ls64, seeds64, avs64, f64 = cpu_sample(np.float64)
+    n64 = max(2, args.steps // 4)
+    t0 = time.perf_counter()
+    o.dp_batch_run([o.dp_params(a=a, **MODEL) for a in avs64], Ls64, seeds64, f64, n64, threads)
+    val64 = sites * n64 / (time.perf_counter() - t0)
     line = {
         "impl": "reference", "metric": METRIC, "value": val,
         "unit": "site-updates/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -224,8 +229,14 @@ def run_reference(args):
         "dtype": "f32", "data": "synthetic",
         "config": dict(workload_config(args.workload), parallelism=f"host threads x{threads}"),
         "cpu_baseline": {"value": val, "unit": "site-updates/s", "cores": threads, "kind": "port",
-                         "sample": f"each step: {n_inst} L=1024 instances of the workload (a cycling over its 16 "
-                                   f"values), {args.steps} timed steps, OpenMP over instances"},
+                         "sample": "each step: one instance per (L, a) of the sweep -- 80 instances, every L in "
+                                   "{64..1024} and every a in the sweep's proportions, 22.3 M sites -- from the "
+                                   "fully active start, FP32 port, OpenMP over instances",
+                         "fp64_port_value": val64,
+                         "fp64_port_sample": f"the same sample in FP64 (the reference's arithmetic), {n64} steps",
+                         "calibration": "on one x86 core the FP32 port runs at 1.03x the reference's own "
+                                        "percolationDornic_2D at its production flags and the FP64 port at 0.81x "
+                                        "(profiles/cpu_reference_vs_port.md)"},
         "e2e": {"value": val, "unit": "site-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

@@ -83,6 +83,8 @@ def lib():
         L.tmo_dornic_consts_compute.argtypes = [C.c_double] * 5 + [C.POINTER(DornicConsts)]
         L.tmo_dp_batch_run_f32.argtypes = [C.POINTER(DPParams), C.POINTER(C.c_int), C.POINTER(C.c_uint64),
                                            C.POINTER(fp), C.c_int, C.c_int64, C.c_int]
+        L.tmo_dp_batch_run_f64.argtypes = [C.POINTER(DPParams), C.POINTER(C.c_int), C.POINTER(C.c_uint64),
+                                           C.POINTER(dp), C.c_int, C.c_int64, C.c_int]
         _lib = L
     return _lib
 
@@ -237,15 +239,23 @@ def rk_run(p, f0, seed, n_steps, meas_steps):
     return mean, act, fin, int(st[0])
 
 
-def dp_batch_run_f32(params, Ls, seeds, fields, n_steps, n_threads=0):
-    """Run independent FP32 DP instances on host threads; fields are updated in place."""
+def dp_batch_run(params, Ls, seeds, fields, n_steps, n_threads=0):
+    """Run independent DP instances on host threads (FP32 or FP64 by the fields'
+    dtype, all alike); fields are updated in place."""
     n = len(Ls)
     P = (DPParams * n)(*params)
     Larr = (C.c_int * n)(*Ls)
     S = (C.c_uint64 * n)(*seeds)
-    ptrs = (C.POINTER(C.c_float) * n)(*[_ptr(f) for f in fields])
-    rc = lib().tmo_dp_batch_run_f32(P, Larr, S, ptrs, n, n_steps, n_threads)
+    f64 = fields[0].dtype == np.float64
+    ptrs = (C.POINTER(C.c_double if f64 else C.c_float) * n)(*[_ptr(f) for f in fields])
+    fn = lib().tmo_dp_batch_run_f64 if f64 else lib().tmo_dp_batch_run_f32
+    rc = fn(P, Larr, S, ptrs, n, n_steps, n_threads)
     assert rc == 0
+
+
+def dp_batch_run_f32(params, Ls, seeds, fields, n_steps, n_threads=0):
+    """Run independent FP32 DP instances on host threads; fields are updated in place."""
+    dp_batch_run(params, Ls, seeds, fields, n_steps, n_threads)
 
 
 _scatter = None

@@ -122,30 +122,32 @@ void tmo_dornic_consts_compute(double lin, double D, double sigma, double dt, do
     o->mean_a2 = a2;
 }
 
-int tmo_dp_batch_run_f32(const tmo_dp_params* p, const int* L, const uint64_t* seed,
-                         float* const* rho, int n_inst, int64_t n_steps, int n_threads)
-{
-    int err = 0;
-#ifdef _OPENMP
-    if (n_threads > 0) omp_set_num_threads(n_threads);
-#pragma omp parallel for schedule(dynamic, 1) reduction(| : err)
-#endif
-    for (int k = 0; k < n_inst; ++k) {
-        int64_t n = (int64_t)L[k] * L[k];
-        float* tmp = (float*)malloc(sizeof(float) * n);
-        if (!tmp) { err |= 1; continue; }
-        float* A = rho[k];
-        float* B = tmp;
-        uint32_t st = 0;
-        for (int64_t s = 0; s < n_steps; ++s) {
-            tmo_dp_step_f32(&p[k], L[k], seed[k], s, A, B, &st);
-            float* t = A; A = B; B = t;
-        }
-        if (A != rho[k]) memcpy(rho[k], A, sizeof(float) * n);
-        free(tmp);
+#define TMO_BATCH_RUN(SFX, TT)                                                                            \
+    int tmo_dp_batch_run_##SFX(const tmo_dp_params* p, const int* L, const uint64_t* seed, TT* const* rho,   \
+                               int n_inst, int64_t n_steps, int n_threads)                                   \
+    {                                                                                                        \
+        int err = 0;                                                                                         \
+        if (n_threads > 0) omp_set_num_threads(n_threads);                                                   \
+        _Pragma("omp parallel for schedule(dynamic, 1) reduction(| : err)")                                  \
+        for (int k = 0; k < n_inst; ++k) {                                                                   \
+            int64_t n = (int64_t)L[k] * L[k];                                                                \
+            TT* tmp = (TT*)malloc(sizeof(TT) * n);                                                           \
+            if (!tmp) { err |= 1; continue; }                                                                \
+            TT* A = rho[k];                                                                                  \
+            TT* B = tmp;                                                                                     \
+            uint32_t st = 0;                                                                                 \
+            for (int64_t s = 0; s < n_steps; ++s) {                                                          \
+                tmo_dp_step_##SFX(&p[k], L[k], seed[k], s, A, B, &st);                                       \
+                TT* t = A; A = B; B = t;                                                                     \
+            }                                                                                                \
+            if (A != rho[k]) memcpy(rho[k], A, sizeof(TT) * n);                                              \
+            free(tmp);                                                                                       \
+        }                                                                                                    \
+        return err ? -1 : 0;                                                                                 \
     }
-    return err ? -1 : 0;
-}
+/* Many independent DP instances on host threads (OpenMP over instances): the CPU baseline. */
+TMO_BATCH_RUN(f32, float)
+TMO_BATCH_RUN(f64, double)
 
 /* FKE advection-diffusion of a consumer field (advdiff_FKE_MultiSp,
  * simulations/Rietkerk_FPE/rietkerk_bjork_FKE.cpp:3614-3695): every site with

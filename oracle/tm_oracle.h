@@ -165,6 +165,8 @@ void tmo_fke_advdiff_f64(int L, const double* rho, const double* gam, const doub
 int tmo_dp_batch_run_f32(const tmo_dp_params* p /* n_inst */, const int* L, const uint64_t* seed,
                          float* const* rho /* in: initial, out: final */, int n_inst,
                          int64_t n_steps, int n_threads);
+int tmo_dp_batch_run_f64(const tmo_dp_params* p, const int* L, const uint64_t* seed,
+                         double* const* rho, int n_inst, int64_t n_steps, int n_threads);
 
 #ifdef __cplusplus
 }

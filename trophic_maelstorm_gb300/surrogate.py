@@ -365,6 +365,49 @@ def critical_point_study(ctx, Ls=(64, 128, 256, 512, 1024), n_a=40, n_rep=15, ju
     return res
 
 
+NU_PERP_DP_2D = 0.733            # correlation-length exponent of 2-D directed percolation (literature value)
+
+
+def critical_point_vs_L(ctx, judge_Ls=(256, 512, 1024), Ls=(64, 128, 256, 512, 1024), n_a=40, n_rep=15,
+                        judge_rep=8, t_max=1000.0, t1=100.0, seed=0):
+    """One corpus and one fitted surrogate, then the guided and the uniform search
+    judged at every side in judge_Ls, and a finite-size extrapolation of the
+    bracket centres: a_c(L) = a_c(inf) + c L^(-1/nu_perp), fitted by least squares
+    (nu_perp of 2-D DP).  The judge's window (t1, t_max) is the same at every L,
+    so a_c(L) is the pseudo-critical point of that window."""
+    import time
+    t0 = time.perf_counter()
+    corpus = training_corpus(ctx, Ls, n_a, n_rep, t_max, seed=seed)
+    t_corpus = time.perf_counter() - t0
+    sur = Surrogate(ctx, seed=seed)
+    loss = sur.fit(corpus)
+    per_L = {}
+    for L in judge_Ls:
+        a_hat = sur.propose(L, t1, t_max)
+        jg = Judge(ctx, L, judge_rep, t_max, t1)
+        g_bracket, g_runs = guided_search(jg, a_hat)
+        ju = Judge(ctx, L, judge_rep, t_max, t1)
+        u_bracket, u_runs = uniform_sweep(ju)
+        per_L[int(L)] = {"a_hat": a_hat, "guided": {"bracket": g_bracket, "runs": g_runs, "seconds": jg.seconds},
+                         "uniform": {"bracket": u_bracket, "runs": u_runs, "seconds": ju.seconds,
+                                     "points": {str(k): v for k, v in sorted(ju.cache.items())}}}
+    sur.close()
+    fit = {}
+    for which in ("guided", "uniform"):
+        pts = [(L, 0.5 * sum(r[which]["bracket"])) for L, r in per_L.items() if r[which]["bracket"]]
+        if len(pts) >= 2:
+            x = np.array([L ** (-1.0 / NU_PERP_DP_2D) for L, _ in pts])
+            y = np.array([a for _, a in pts])
+            A = np.stack([np.ones_like(x), x], 1)
+            coef, *_ = np.linalg.lstsq(A, y, rcond=None)
+            fit[which] = {"a_c_inf": float(coef[0]), "c": float(coef[1]), "centres": {str(L): a for L, a in pts}}
+    return {"judge": {"replicates": judge_rep, "t1": t1, "t_max": t_max, "delta_DP": DELTA_DP_2D},
+            "corpus": {"Ls": list(Ls), "a_per_L": n_a, "replicates": n_rep, "runs": corpus.runs,
+                       "site_updates": corpus.site_updates, "seconds": t_corpus},
+            "fit_loss_last": float(loss[-1]), "per_L": per_L, "extrapolation": fit,
+            "nu_perp": NU_PERP_DP_2D}
+
+
 def main():
     import argparse
     import json
@@ -376,8 +419,15 @@ def main():
     ap.add_argument("--judge-rep", type=int, default=8)
     ap.add_argument("--t-max", type=float, default=1000.0)
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--judge-Ls", default="", help="comma list: judge at every side and extrapolate a_c(L)")
     a = ap.parse_args()
     ctx = api.Context(0)
+    if a.judge_Ls:
+        res = critical_point_vs_L(ctx, tuple(int(x) for x in a.judge_Ls.split(",")),
+                                  tuple(int(x) for x in a.Ls.split(",")), a.n_a, a.n_rep, a.judge_rep, a.t_max,
+                                  a.t_max / 10, a.seed)
+        print(json.dumps(res))
+        return
     res = critical_point_study(ctx, tuple(int(x) for x in a.Ls.split(",")), a.n_a, a.n_rep, a.judge_L,
                                a.judge_rep, a.t_max, a.t_max / 10, a.seed)
     print(json.dumps(res))
