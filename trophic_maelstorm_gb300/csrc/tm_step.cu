@@ -8,8 +8,11 @@
 // site-update in FP32).  Sites that need a random draw are compacted into a
 // per-warp queue in shared memory so that every lane of the sampler loop works
 // on a live site: absorbing sites never occupy a sampler lane.  FP32 draws take
-// a straight-line path first; the few sites it defers are carried from task to
-// task and drawn by the general sampler 32 at a time.  Per site it fuses:
+// a straight-line path first; the few sites it defers (about 2 % of live sites)
+// go to a global list that a second kernel draws with the general sampler, so
+// the step kernel's loop body holds no general-sampler code.  FP64 draws every
+// live site with the general sampler, carried from task to task and drawn 32 at
+// a time.  Per site it fuses:
 //   alpha_i  = (D/dx^2) * sum of the 4 neighbours       stochasticSPDP.cpp:1037-1038
 //   skip     if alpha_i == 0 and rho_i == 0             :1049-1052
 //   rho*     = Gamma(2 alpha_i/sigma^2 + Poisson(lambda e^{beta dt} rho_i)) / lambda   :1053-1059
@@ -119,9 +122,9 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
     const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int nw = (int)((gridDim.x * blockDim.x) >> 5);
     const long long step = (A.step_base ? *A.step_base : 0LL) + A.step_off;
-    int nc = 0;  // entries carried in Ck/Cs/Cm/Cmu
-    // One more trip after the last task draws the carried entries; the general
-    // sampler has a single call site, so its code is in the loop body once.
+    int nc = 0;  // entries carried in Ck/Cs/Cm/Cmu (FP64)
+    // FP64: one more trip after the last task draws the carried entries; the
+    // general sampler has a single call site, so its code is in the loop body once.
     for (int t = gw;; t += nw) {
         const bool more = t < A.n_tasks;
         int k = 0, L = 0, x0 = 0, y0 = 0, ndef = 0;
@@ -205,9 +208,18 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
                         if (deferred) atomicOr(Wrows + (li & 31), 1u << (li >> 5));
                         else Wres[li] = v;
                     }
+                    // deferred sites: appended to the batch's list (one atomic per warp)
                     const unsigned bal = __ballot_sync(0xffffffffu, has && deferred);
-                    if (has && deferred) Wdef[ndef + __popc(bal & lt_mask)] = (unsigned short)j;
-                    ndef += __popc(bal);
+                    if (bal) {
+                        unsigned at = 0;
+                        if (lane == 0) at = atomicAdd(A.dcount, (unsigned)__popc(bal));
+                        at = __shfl_sync(0xffffffffu, at, 0);
+                        if (has && deferred) {
+                            const int li = Wqi[j];
+                            A.dlist[at + __popc(bal & lt_mask)] =
+                                make_uint2((unsigned)k, (unsigned)((y0 + (li >> 5)) * L + x0 + (li & 31)));
+                        }
+                    }
                 }
                 __syncwarp();
                 drows = Wrows[lane];
@@ -235,9 +247,14 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
             }
             if (st) atomicOr(A.it.status + k, st);
         }
-        // general sampler: the carried sites, then this task's list, 32 per
+        // FP64 general sampler: the carried sites, then this task's list, 32 per
         // pass so that every lane draws; fewer than 32 are carried on (all of
         // them on the trip after the last task)
+        if constexpr (sizeof(T) == 4) {
+            if (!more) break;
+            __syncwarp();
+            continue;
+        }
         const int tot = nc + ndef;
         const int lim = more ? (tot & ~31) : tot;
         for (int done = 0; done < lim; done += 32) {
@@ -278,6 +295,35 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
     }
 }
 
+// The FP32 sites the straight-line draw deferred, drawn by the general sampler:
+// each list entry (instance, site) re-forms its Poisson mean and Gamma shape from
+// the input lattice with pass 1's arithmetic, so the draw is the one the step
+// kernel would have made.  Grid-stride over the count the step kernel left.
+template <typename T, int REM, int SAMP, int CAP>
+__global__ void __launch_bounds__(256) dornic_deferred_kernel(const DornicArgs<T> A)
+{
+    __shared__ SmemTab<T> tab;
+    tab.fill();
+    __syncthreads();
+    const unsigned n = *A.dcount;
+    const long long step = (A.step_base ? *A.step_base : 0LL) + A.step_off;
+    for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        const uint2 d = A.dlist[e];
+        const int k = (int)d.x;
+        const int L = A.it.L[k];
+        const int y = (int)(d.y / (unsigned)L), x = (int)d.y - y * L;
+        const int yn = y == 0 ? L - 1 : y - 1, ys = y == L - 1 ? 0 : y + 1;
+        const int xw = x == 0 ? L - 1 : x - 1, xe = x == L - 1 ? 0 : x + 1;
+        const T* __restrict__ src = A.in + A.it.off[k];
+        const T cur = src[d.y];
+        const T nsum = ((src[(long long)yn * L + x] + src[(long long)ys * L + x]) + src[(long long)y * L + xw]) +
+                       src[(long long)y * L + xe];
+        const T alpha = A.dcoef * nsum;
+        const T pm = (T)A.it.consts[k].x;
+        draw_general_site<T, REM, SAMP, CAP>(A, tab, step, k, d.y, pm * cur, alpha * A.two_s2);
+    }
+}
+
 template <typename T, int REM, int SAMP, int CAP = kSamplerCap>
 cudaError_t launch_dornic_t(const DornicArgs<T>& a, int grid, int block, size_t smem, cudaStream_t s)
 {
@@ -289,7 +335,13 @@ cudaError_t launch_dornic_t(const DornicArgs<T>& a, int grid, int block, size_t 
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
+    if constexpr (sizeof(T) == 4) {
+        if (a.dlist == nullptr || a.dcount == nullptr) return cudaErrorInvalidValue;
+        const cudaError_t e = cudaMemsetAsync(a.dcount, 0, sizeof(unsigned), s);
+        if (e != cudaSuccess) return e;
+    }
     dornic_step_kernel<T, REM, SAMP, CAP><<<grid, block, smem, s>>>(a);
+    if constexpr (sizeof(T) == 4) dornic_deferred_kernel<T, REM, SAMP, CAP><<<a.deferred_grid, 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 
