@@ -155,7 +155,11 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
             T north = act ? src[(long long)yn * L + x] : T(0);
             T cur = act ? src[(long long)y0 * L + x] : T(0);
             T south = act ? src[(long long)((y0 == L - 1) ? 0 : y0 + 1) * L + x] : T(0);
-            int nq = 0;
+            // FP32 with the exact sampler keeps the live-site queue two-ended: sites
+            // in split_region from the front, the others from the back, so that a
+            // 32-site chunk of pass 2 mixes the two draws at most once per task
+            constexpr bool kTwoEnded = sizeof(T) == 4 && SAMP == 0;
+            int nq = 0, ns = 0, np = 0;
             unsigned drows = 0;  // rows of this lane's column left to the general sampler
             Wrows[lane] = 0u;
             for (int r = 0; r < rows; ++r) {
@@ -179,13 +183,28 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
                 const unsigned bal = __ballot_sync(0xffffffffu, live);
                 if (!live) Wres[r * 32 + lane] = (SAMP == 2 && act) ? a1 * cur + a2 * alpha : T(0);
                 if (sizeof(T) == 8 && live) drows |= 1u << r;
-                if (live) {
-                    const int pos = nq + __popc(bal & lt_mask);
-                    Wqi[pos] = (unsigned short)(r * 32 + lane);
-                    Wqm[pos] = pm * cur;
-                    Wqmu[pos] = alpha * A.two_s2;
+                if constexpr (kTwoEnded) {
+                    const T mq = pm * cur, muq = alpha * A.two_s2;
+                    const unsigned bs = __ballot_sync(0xffffffffu, live && split_region(mq, muq));
+                    if (live) {
+                        const bool sp = (bs >> lane) & 1u;
+                        const int pos = sp ? ns + __popc(bs & lt_mask) : cap - 1 - (np + __popc(bal & ~bs & lt_mask));
+                        Wqi[pos] = (unsigned short)(r * 32 + lane);
+                        Wqm[pos] = mq;
+                        Wqmu[pos] = muq;
+                    }
+                    ns += __popc(bs);
+                    np += __popc(bal & ~bs);
+                    nq = ns + np;
+                } else {
+                    if (live) {
+                        const int pos = nq + __popc(bal & lt_mask);
+                        Wqi[pos] = (unsigned short)(r * 32 + lane);
+                        Wqm[pos] = pm * cur;
+                        Wqmu[pos] = alpha * A.two_s2;
+                    }
+                    nq += __popc(bal);
                 }
-                nq += __popc(bal);
                 north = cur;
                 cur = south;
                 south = next;
@@ -197,14 +216,21 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
             const unsigned long long seed = A.it.seed[k];
             if constexpr (sizeof(T) == 4) {
                 for (int base = 0; base < nq; base += 32) {
-                    const int j = base + lane;
-                    const bool has = j < nq;
+                    const int jv = base + lane;
+                    const bool has = jv < nq;
+                    // queue entry: the split sites [0, ns), then the others [cap - np, cap)
+                    const int j = (!kTwoEnded || jv < ns) ? jv : cap - np + (jv - ns);
                     bool deferred = false;
                     if (has) {
                         const int li = Wqi[j];
                         const int site = (y0 + (li >> 5)) * L + x0 + (li & 31);
-                        const float v = dornic_draw_fast(seed, (uint32_t)site, step, Wqm[j], Wqmu[j], inv_lambda,
-                                                         SAMP, tab, deferred);
+                        float v;
+                        if (kTwoEnded && jv < ns)
+                            v = dornic_draw_fast_split(seed, (uint32_t)site, step, Wqm[j], Wqmu[j], inv_lambda, tab,
+                                                       deferred);
+                        else
+                            v = dornic_draw_fast(seed, (uint32_t)site, step, Wqm[j], Wqmu[j], inv_lambda, SAMP, tab,
+                                                 deferred);
                         if (deferred) atomicOr(Wrows + (li & 31), 1u << (li >> 5));
                         else Wres[li] = v;
                     }
