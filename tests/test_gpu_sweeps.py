@@ -92,10 +92,14 @@ def test_fss_collapse_rows_equal_single_size_runs(tmg, ctx):
 
 
 def test_fss_stationary_windows(tmg, ctx):
+    """Sides from the reference's lnspace, cast to int as it does (lnspace(40, 60, 2)
+    starts at 39.999..., so side 39), each measured on its window."""
     rows, st = tmg.critical_exp_finite_scaling_stationary(2, 40, 60, 0.0, 0.0, 0.53, 2.0, 1.0, 1.0, 0.1, 1.0, 2,
                                                           precision=tmg.TM_FP32, ctx=ctx)
     assert not st.any()
-    for g, (t0, t1) in ((40, (300.0, 900.0)), (60, (1000.0, 2500.0))):
+    sides = [int(g) for g in tmg.api.lnspace(40, 60, 2)]
+    assert sides == [39, 60] and sorted(set(rows[:, 1].astype(int))) == sides
+    for g, (t0, t1) in zip(sides, ((300.0, 900.0), (1000.0, 2500.0))):
         ts = rows[rows[:, 1] == g][:, 2]
         late = ts[ts > 1.0]
         assert np.allclose(late, tmg.linspace(t0, t1, 30), rtol=0, atol=1e-9)
