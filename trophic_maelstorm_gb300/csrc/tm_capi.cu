@@ -66,8 +66,9 @@ struct tm_batch {
     void* buf[2] = {nullptr, nullptr};
     int cur = 0;
     void* aux = nullptr;        // Rietkerk P* (field-0 slots)
-    uint2* d_dlist = nullptr;   // FP32: sites the straight-line draw deferred (one entry per field-0 site at most)
-    unsigned* d_dcount = nullptr;
+    uint4* d_dlist = nullptr;   // FP32: sites the straight-line draw deferred, a segment per warp of the grid
+    unsigned* d_dcnt = nullptr;
+    long long dlist_cap = 0, max_seg = 0;
     void* site_b = nullptr;     // per-site loss coefficient (DP), packed like the state
     long long* d_step = nullptr;
     int64_t step = 0;
@@ -173,6 +174,17 @@ int build_tasks(tm_batch* b)
         TM_CUDA(dalloc(&b->d_btasks, bt.size()));
         TM_CUDA(cudaMemcpy(b->d_btasks, bt.data(), bt.size() * sizeof(int4), cudaMemcpyHostToDevice));
     }
+    if (b->precision == TM_FP32) {
+        // the deferred-site list: a step grid of nw warps gives every warp a segment of
+        // ceil(n_tasks / nw) tasks' sites, nw * that <= (n_tasks + nw) * R * 32 entries;
+        // sized for the largest grid (64 CTAs of 8 warps per SM, at most one warp per task)
+        cudaFree(b->d_dlist); b->d_dlist = nullptr;
+        cudaFree(b->d_dcnt); b->d_dcnt = nullptr;
+        b->max_seg = std::min<long long>((long long)b->n_tasks + 8, (long long)std::max(1, b->ctx->num_sms) * 64 * 8);
+        b->dlist_cap = ((long long)b->n_tasks + b->max_seg) * R * 32;
+        TM_CUDA(dalloc(&b->d_dlist, (size_t)b->dlist_cap));
+        TM_CUDA(dalloc(&b->d_dcnt, (size_t)b->max_seg));
+    }
     free_graphs(b);
     return TM_OK;
 }
@@ -193,8 +205,13 @@ DornicArgs<T> dornic_args(const tm_batch* b, const T* in, T* out, const long lon
     a.step_base = step_base; a.step_off = step_off; a.rows_cap = b->rows_per_task;
     a.cap1 = (b->probe & TM_PROBE_SAMPLER_CAP1) ? 1 : 0;
     a.dlist = b->d_dlist;
-    a.dcount = b->d_dcount;
-    a.deferred_grid = std::max(1, 2 * b->ctx->num_sms);
+    a.dcnt = b->d_dcnt;
+    a.dlist_cap = b->dlist_cap;
+    a.max_seg = b->max_seg;
+    {   // one list segment per warp of the step grid, holding all sites of that warp's tasks
+        const long long nw = (long long)warp_grid(b, b->n_tasks) * 8;
+        a.seg_cap = ((long long)b->n_tasks + nw - 1) / nw * b->rows_per_task * 32;
+    }
     a.site_b = (b->model == 0) ? (const T*)b->site_b : nullptr;
     if (b->model == 0) {
         const tm_dp_model& m = b->dpm;
@@ -390,14 +407,7 @@ int batch_common_init(tm_batch* b, const tm_instance* inst, int n)
     TM_CUDA(cudaMemcpy(b->d_alive, ones.data(), n * sizeof(int), cudaMemcpyHostToDevice));
     TM_CUDA(cudaMemset(b->d_status, 0, n * sizeof(unsigned)));
     TM_CUDA(cudaMemset(b->d_step, 0, sizeof(long long)));
-    if (b->precision == TM_FP32) {
-        // the deferred-site list: at most every field-0 site of every instance, once per step
-        size_t sites = 0;
-        for (int k = 0; k < n; ++k) sites += (size_t)inst[k].L * inst[k].L;
-        TM_CUDA(dalloc(&b->d_dlist, sites));
-        TM_CUDA(dalloc(&b->d_dcount, 1));
-        TM_CUDA(cudaMemset(b->d_dcount, 0, sizeof(unsigned)));
-    }
+
     b->probe = b->ctx->probe;
     b->rows_per_task = default_rows(b);
     return build_tasks(b);
@@ -501,7 +511,7 @@ int tm_batch_destroy(tm_batch* b)
     cudaStreamSynchronize(b->ctx->stream);
     free_graphs(b);
     cudaFree(b->buf[0]); cudaFree(b->buf[1]); cudaFree(b->aux); cudaFree(b->site_b);
-    cudaFree(b->d_dlist); cudaFree(b->d_dcount);
+    cudaFree(b->d_dlist); cudaFree(b->d_dcnt);
     cudaFree(b->d_step); cudaFree(b->d_off); cudaFree(b->d_fstride); cudaFree(b->d_L); cudaFree(b->d_seed);
     cudaFree(b->d_R); cudaFree(b->d_a0); cudaFree(b->d_astep); cudaFree(b->d_consts); cudaFree(b->d_alive);
     cudaFree(b->d_status); cudaFree(b->d_tasks); cudaFree(b->d_task_begin); cudaFree(b->d_btasks);

@@ -533,33 +533,11 @@ __device__ __forceinline__ T gamma_draw(Stream<T>& g, T k, int sampler, const Sm
     return gamma_mt<CAP>(g, k, tb);
 }
 
-// Region of the normal-plus-Gamma form of the exact draw (see dornic_draw).
-constexpr float kSplitM = 4.0f, kSplitMu1 = 1.5f;
-template <typename T>
-__device__ __forceinline__ bool split_region(T m, T mu1)
-{
-    return m >= T(kSplitM) && mu1 >= T(kSplitMu1);
-}
-
-// rho* = Gamma(mu1 + Poisson(m)) / lambda  (stochasticSPDP.cpp:1053-1059).  With
-// the exact sampler in split_region the same law is drawn as
-//   (Z + sqrt(2m))^2 / 2 + Gamma(mu1 - 1/2):
-// 2 Gamma(mu1 + Poisson(m)) is noncentral chi-square with 2 mu1 degrees of
-// freedom and noncentrality 2m, which for 2 mu1 > 1 splits into the square of a
-// normal of mean sqrt(2m) and an independent central chi-square with 2 mu1 - 1
-// degrees of freedom (Broadie & Kaya 2006).  One normal replaces a count search
-// whose length grows with m; the shape mu1 - 1/2 >= 1 needs no boost.
+// rho* = Gamma(mu1 + Poisson(m)) / lambda  (stochasticSPDP.cpp:1053-1059)
 template <int CAP, typename T>
 __device__ __forceinline__ T dornic_draw(Stream<T>& g, T m, T mu1, T inv_lambda, int sampler,
                                         const SmemTab<T>& tb)
 {
-    if (sampler == 0 && split_region(m, mu1)) {
-        const T z = g.template normal<CAP>(tb);
-        const T t = z + Tr<T>::sqrt_(T(2) * m);
-        const T part = (t * t) * T(0.5);
-        const T gv = gamma_mt<CAP>(g, mu1 - T(0.5), tb);
-        return (part + gv) * inv_lambda;
-    }
     const T n = poisson_draw<CAP>(g, m, sampler, tb);
     const T k = mu1 + n;
     const T gv = gamma_draw<CAP>(g, k, sampler, tb);
@@ -661,40 +639,6 @@ __device__ __forceinline__ float dornic_draw_fast(uint64_t seed, uint32_t site, 
         res = res * tm_exp(tm_log_pos(ub) / k);
     }
     return res * inv_lambda;
-}
-
-// Straight-line draw of the split form (FP32, exact sampler, split_region):
-// word 0 is Z by the ziggurat's fast test, words 1 and 2 the Gamma attempt's
-// normal and uniform, as dornic_draw consumes them; the rest is deferred.
-__device__ __forceinline__ float dornic_draw_fast_split(uint64_t seed, uint32_t site, int64_t step, float m, float mu1,
-                                                        float inv_lambda, const SmemTab<float>& tb, bool& deferred)
-{
-    deferred = false;
-    const U4 r = philox4x32_10(site, (uint32_t)(uint64_t)step, 0u, (uint32_t)((uint64_t)step >> 32),
-                               (uint32_t)seed, (uint32_t)(seed >> 32));
-    const int i0 = zig_layer(r.x);
-    const int32_t h0 = zig_value(r.x);
-    const uint32_t a0 = (uint32_t)(h0 < 0 ? -h0 : h0);
-    const ZigLayer<float> l0 = tb.zig[i0];
-    if (!(a0 < l0.k)) { deferred = true; return 0.0f; }
-    const float t = (float)h0 * l0.w + sqrtf(2.0f * m);
-    const float part = (t * t) * 0.5f;
-    const float d = (mu1 - 0.5f) - (float)(1.0 / 3.0);
-    const float c = Tr<float>::inv_sqrt(9.0f * d);
-    const int i1 = zig_layer(r.y);
-    const int32_t h1 = zig_value(r.y);
-    const uint32_t a1 = (uint32_t)(h1 < 0 ? -h1 : h1);
-    const ZigLayer<float> l1 = tb.zig[i1];
-    if (!(a1 < l1.k)) { deferred = true; return 0.0f; }
-    const float x = (float)h1 * l1.w;
-    float v = 1.0f + c * x;
-    if (!(v > 0.0f)) { deferred = true; return 0.0f; }
-    const float mm = (v < 1.0f) ? v : 1.0f;
-    v = (v * v) * v;
-    const float u = ((float)(r.z >> 8) + 0.5f) * 0x1p-24f;
-    const float x2 = x * x;
-    if (!((1.0f - u) * ((108.0f * d) * mm) > x2 * x2)) { deferred = true; return 0.0f; }
-    return (part + d * v) * inv_lambda;
 }
 
 template <typename T>

@@ -48,9 +48,12 @@ struct DornicArgs {
     const T* site_b;               // per-site loss coefficient b_v (packed like the state) or nullptr
     int zero_fixed;                // a +0 draw finishes as +0, no status bit (finite b, c, dt; no site_b)
     int cap1;                      // TM_PROBE_SAMPLER_CAP1: rejection loops stop after one attempt
-    uint2* dlist;                  // FP32: (instance, site) of each deferred site, one per live site at most
-    unsigned* dcount;              // FP32: entries in dlist (zeroed before each step)
-    int deferred_grid;             // FP32: CTAs of the deferred-site kernel
+    uint4* dlist;                  // FP32: deferred sites (instance, site, Poisson mean, Gamma shape bits),
+                                   // one segment of seg_cap entries per warp of the step kernel's grid
+    unsigned* dcnt;                // FP32: entries in each warp's segment (written by the step kernel)
+    long long seg_cap;             // entries per segment (all sites of one warp's tasks)
+    long long dlist_cap;           // entries the list holds
+    long long max_seg;             // segments dcnt holds
 };
 
 template <typename T>

@@ -8,9 +8,10 @@
 // site-update in FP32).  Sites that need a random draw are compacted into a
 // per-warp queue in shared memory so that every lane of the sampler loop works
 // on a live site: absorbing sites never occupy a sampler lane.  FP32 draws take
-// a straight-line path first; the few sites it defers (about 2 % of live sites)
-// go to a global list that a second kernel draws with the general sampler, so
-// the step kernel's loop body holds no general-sampler code.  FP64 draws every
+// a straight-line path first; the few sites it defers (a few % of live sites)
+// go to the warp's own segment of a batch-wide list (no atomics: the warp keeps
+// the count) that a second kernel draws with the general sampler, so the step
+// kernel's loop body holds no general-sampler code.  FP64 draws every
 // live site with the general sampler, carried from task to task and drawn 32 at
 // a time.  Per site it fuses:
 //   alpha_i  = (D/dx^2) * sum of the 4 neighbours       stochasticSPDP.cpp:1037-1038
@@ -123,6 +124,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
     const int nw = (int)((gridDim.x * blockDim.x) >> 5);
     const long long step = (A.step_base ? *A.step_base : 0LL) + A.step_off;
     int nc = 0;  // entries carried in Ck/Cs/Cm/Cmu (FP64)
+    int nseg = 0;  // entries in this warp's segment of the deferred-site list (FP32)
     // FP64: one more trip after the last task draws the carried entries; the
     // general sampler has a single call site, so its code is in the loop body once.
     for (int t = gw;; t += nw) {
@@ -155,11 +157,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
             T north = act ? src[(long long)yn * L + x] : T(0);
             T cur = act ? src[(long long)y0 * L + x] : T(0);
             T south = act ? src[(long long)((y0 == L - 1) ? 0 : y0 + 1) * L + x] : T(0);
-            // FP32 with the exact sampler keeps the live-site queue two-ended: sites
-            // in split_region from the front, the others from the back, so that a
-            // 32-site chunk of pass 2 mixes the two draws at most once per task
-            constexpr bool kTwoEnded = sizeof(T) == 4 && SAMP == 0;
-            int nq = 0, ns = 0, np = 0;
+            int nq = 0;
             unsigned drows = 0;  // rows of this lane's column left to the general sampler
             Wrows[lane] = 0u;
             for (int r = 0; r < rows; ++r) {
@@ -183,28 +181,13 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
                 const unsigned bal = __ballot_sync(0xffffffffu, live);
                 if (!live) Wres[r * 32 + lane] = (SAMP == 2 && act) ? a1 * cur + a2 * alpha : T(0);
                 if (sizeof(T) == 8 && live) drows |= 1u << r;
-                if constexpr (kTwoEnded) {
-                    const T mq = pm * cur, muq = alpha * A.two_s2;
-                    const unsigned bs = __ballot_sync(0xffffffffu, live && split_region(mq, muq));
-                    if (live) {
-                        const bool sp = (bs >> lane) & 1u;
-                        const int pos = sp ? ns + __popc(bs & lt_mask) : cap - 1 - (np + __popc(bal & ~bs & lt_mask));
-                        Wqi[pos] = (unsigned short)(r * 32 + lane);
-                        Wqm[pos] = mq;
-                        Wqmu[pos] = muq;
-                    }
-                    ns += __popc(bs);
-                    np += __popc(bal & ~bs);
-                    nq = ns + np;
-                } else {
-                    if (live) {
-                        const int pos = nq + __popc(bal & lt_mask);
-                        Wqi[pos] = (unsigned short)(r * 32 + lane);
-                        Wqm[pos] = pm * cur;
-                        Wqmu[pos] = alpha * A.two_s2;
-                    }
-                    nq += __popc(bal);
+                if (live) {
+                    const int pos = nq + __popc(bal & lt_mask);
+                    Wqi[pos] = (unsigned short)(r * 32 + lane);
+                    Wqm[pos] = pm * cur;
+                    Wqmu[pos] = alpha * A.two_s2;
                 }
+                nq += __popc(bal);
                 north = cur;
                 cur = south;
                 south = next;
@@ -216,36 +199,26 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
             const unsigned long long seed = A.it.seed[k];
             if constexpr (sizeof(T) == 4) {
                 for (int base = 0; base < nq; base += 32) {
-                    const int jv = base + lane;
-                    const bool has = jv < nq;
-                    // queue entry: the split sites [0, ns), then the others [cap - np, cap)
-                    const int j = (!kTwoEnded || jv < ns) ? jv : cap - np + (jv - ns);
+                    const int j = base + lane;
+                    const bool has = j < nq;
                     bool deferred = false;
                     if (has) {
                         const int li = Wqi[j];
                         const int site = (y0 + (li >> 5)) * L + x0 + (li & 31);
-                        float v;
-                        if (kTwoEnded && jv < ns)
-                            v = dornic_draw_fast_split(seed, (uint32_t)site, step, Wqm[j], Wqmu[j], inv_lambda, tab,
-                                                       deferred);
-                        else
-                            v = dornic_draw_fast(seed, (uint32_t)site, step, Wqm[j], Wqmu[j], inv_lambda, SAMP, tab,
-                                                 deferred);
+                        const float v = dornic_draw_fast(seed, (uint32_t)site, step, Wqm[j], Wqmu[j], inv_lambda,
+                                                         SAMP, tab, deferred);
                         if (deferred) atomicOr(Wrows + (li & 31), 1u << (li >> 5));
                         else Wres[li] = v;
                     }
-                    // deferred sites: appended to the batch's list (one atomic per warp)
+                    // deferred sites: appended to this warp's segment of the list
                     const unsigned bal = __ballot_sync(0xffffffffu, has && deferred);
-                    if (bal) {
-                        unsigned at = 0;
-                        if (lane == 0) at = atomicAdd(A.dcount, (unsigned)__popc(bal));
-                        at = __shfl_sync(0xffffffffu, at, 0);
-                        if (has && deferred) {
-                            const int li = Wqi[j];
-                            A.dlist[at + __popc(bal & lt_mask)] =
-                                make_uint2((unsigned)k, (unsigned)((y0 + (li >> 5)) * L + x0 + (li & 31)));
-                        }
+                    if (has && deferred) {
+                        const int li = Wqi[j];
+                        A.dlist[(long long)gw * A.seg_cap + nseg + __popc(bal & lt_mask)] =
+                            make_uint4((unsigned)k, (unsigned)((y0 + (li >> 5)) * L + x0 + (li & 31)),
+                                       __float_as_uint(Wqm[j]), __float_as_uint(Wqmu[j]));
                     }
+                    nseg += __popc(bal);
                 }
                 __syncwarp();
                 drows = Wrows[lane];
@@ -277,7 +250,10 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
         // pass so that every lane draws; fewer than 32 are carried on (all of
         // them on the trip after the last task)
         if constexpr (sizeof(T) == 4) {
-            if (!more) break;
+            if (!more) {
+                if (lane == 0) A.dcnt[gw] = (unsigned)nseg;
+                break;
+            }
             __syncwarp();
             continue;
         }
@@ -321,32 +297,27 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
     }
 }
 
-// The FP32 sites the straight-line draw deferred, drawn by the general sampler:
-// each list entry (instance, site) re-forms its Poisson mean and Gamma shape from
-// the input lattice with pass 1's arithmetic, so the draw is the one the step
-// kernel would have made.  Grid-stride over the count the step kernel left.
+// The FP32 sites the straight-line draw deferred, drawn by the general sampler
+// from their list entries (instance, site, Poisson mean, Gamma shape): one warp
+// per segment of the step kernel's grid, 32 entries at a time.
 template <typename T, int REM, int SAMP, int CAP>
-__global__ void __launch_bounds__(256) dornic_deferred_kernel(const DornicArgs<T> A)
+__global__ void __launch_bounds__(256) dornic_deferred_kernel(const DornicArgs<T> A, int n_seg)
 {
     __shared__ SmemTab<T> tab;
     tab.fill();
     __syncthreads();
-    const unsigned n = *A.dcount;
     const long long step = (A.step_base ? *A.step_base : 0LL) + A.step_off;
-    for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
-        const uint2 d = A.dlist[e];
-        const int k = (int)d.x;
-        const int L = A.it.L[k];
-        const int y = (int)(d.y / (unsigned)L), x = (int)d.y - y * L;
-        const int yn = y == 0 ? L - 1 : y - 1, ys = y == L - 1 ? 0 : y + 1;
-        const int xw = x == 0 ? L - 1 : x - 1, xe = x == L - 1 ? 0 : x + 1;
-        const T* __restrict__ src = A.in + A.it.off[k];
-        const T cur = src[d.y];
-        const T nsum = ((src[(long long)yn * L + x] + src[(long long)ys * L + x]) + src[(long long)y * L + xw]) +
-                       src[(long long)y * L + xe];
-        const T alpha = A.dcoef * nsum;
-        const T pm = (T)A.it.consts[k].x;
-        draw_general_site<T, REM, SAMP, CAP>(A, tab, step, k, d.y, pm * cur, alpha * A.two_s2);
+    const int lane = threadIdx.x & 31;
+    const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int nw = (int)((gridDim.x * blockDim.x) >> 5);
+    for (int w = gw; w < n_seg; w += nw) {
+        const int n = (int)A.dcnt[w];
+        const uint4* seg = A.dlist + (long long)w * A.seg_cap;
+        for (int i = lane; i < n; i += 32) {
+            const uint4 d = seg[i];
+            draw_general_site<T, REM, SAMP, CAP>(A, tab, step, (int)d.x, d.y, __uint_as_float(d.z),
+                                                 __uint_as_float(d.w));
+        }
     }
 }
 
@@ -361,13 +332,16 @@ cudaError_t launch_dornic_t(const DornicArgs<T>& a, int grid, int block, size_t 
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
+    const int n_seg = grid * (block >> 5);   // one list segment per warp of the step kernel
     if constexpr (sizeof(T) == 4) {
-        if (a.dlist == nullptr || a.dcount == nullptr) return cudaErrorInvalidValue;
-        const cudaError_t e = cudaMemsetAsync(a.dcount, 0, sizeof(unsigned), s);
-        if (e != cudaSuccess) return e;
+        // every warp's segment must hold all sites of its tasks
+        const long long need = ((long long)a.n_tasks + n_seg - 1) / n_seg * a.rows_cap * 32;
+        if (a.dlist == nullptr || a.dcnt == nullptr || need > a.seg_cap || (long long)n_seg > a.max_seg ||
+            (long long)n_seg * a.seg_cap > a.dlist_cap)
+            return cudaErrorInvalidValue;
     }
     dornic_step_kernel<T, REM, SAMP, CAP><<<grid, block, smem, s>>>(a);
-    if constexpr (sizeof(T) == 4) dornic_deferred_kernel<T, REM, SAMP, CAP><<<a.deferred_grid, 256, 0, s>>>(a);
+    if constexpr (sizeof(T) == 4) dornic_deferred_kernel<T, REM, SAMP, CAP><<<(n_seg + 7) / 8, 256, 0, s>>>(a, n_seg);
     return cudaGetLastError();
 }
 
