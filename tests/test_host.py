@@ -109,9 +109,23 @@ def test_invalid_arguments_are_rejected_without_gpu(tmlib):
         "tm_mlp_loss_grad": (None, 1.0, None, None),
         "tm_mlp_train": (None, 1, 1e-3, 0.9, 0.999, 1e-8, 1.0, None),
         "tm_mlp_predict": (None, None, 0, None),
+        "tm_set_test_probe": (None, 0),
+        "tm_batch_set_spreading": (None, 1, -1, -1),
+        "tm_fke_advdiff_device_ws": (None, None, None, None, 1, 0, 1.0, 1e-10, None, 1, None, 1, None, None, 0,
+                                     None),
     }
     for name, args in calls.items():
         assert getattr(L, name)(*args) == bad, name
+    # workspace sizing needs no device: 0 for an impossible request, else the five L^2 arrays,
+    # the two wrapped stencils and the counter, each on a 256-byte boundary
+    assert L.tm_fke_workspace_bytes(7, 64) == 0 and L.tm_fke_workspace_bytes(tmlib.TM_FP64, 0) == 0
+    a256 = lambda v: (v + 255) // 256 * 256
+    for prec, es in ((tmlib.TM_FP64, 8), (tmlib.TM_FP32, 4)):
+        for n in (1, 33, 1024):
+            o = 0
+            for size in (n * n * es, n * n * es, n * n * es, n * n * 4, n * n * 4, n * es, n * es):
+                o = a256(o + size)
+            assert L.tm_fke_workspace_bytes(prec, n) == o + 256
 
 
 def test_lnspace_matches_reference():
