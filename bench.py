@@ -520,11 +520,24 @@ def run_ours(args):
     barrier(world)
     st = np.zeros(0, np.uint32)
     e2e = None
+    e2e_reps = []
     if not args.no_e2e:
-        t0 = time.perf_counter()
+        # one untimed pass through the same calls, then five timed ones (median reported, each
+        # repetition's upload and advance times kept in the line: the host-to-device copy of the
+        # 2.86 GB state shares the host link with the machine's other jobs and varies by 10x)
         b.upload(hv, step=0)
-        obs, st = b.advance(e_steps, [0, e_steps])
-        e2e_s = time.perf_counter() - t0
+        b.advance(e_steps, [0, e_steps])
+        for _ in range(5):
+            torch.cuda.synchronize()
+            barrier(world)
+            t0 = time.perf_counter()
+            b.upload(hv, step=0)
+            t1 = time.perf_counter()
+            obs, st = b.advance(e_steps, [0, e_steps])
+            t2 = time.perf_counter()
+            e2e_reps.append({"total_s": t2 - t0, "upload_s": t1 - t0, "advance_s": t2 - t1,
+                             "upload_gbs": total * 4 / (t1 - t0) / 1e9})
+        e2e_s = statistics.median(r["total_s"] for r in e2e_reps)
         e2e_s = max_over_ranks(e2e_s, world)
         e2e = sites * e_steps * world / e2e_s
 
@@ -563,7 +576,9 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "e2e": None if e2e is None else {"value": e2e, "unit": "site-updates/s",
                                              "h2d_bytes_per_step": total * 4 / e_steps,
-                                             "d2h_bytes_per_step": obs_bytes / e_steps, "steps": e_steps},
+                                             "d2h_bytes_per_step": obs_bytes / e_steps, "steps": e_steps,
+                                             "timing": "median of 5 after one untimed pass",
+                                             "repetitions": e2e_reps},
             "gpu_launches": 2 * args.steps,   # per step: the step kernel and the deferred-site kernel
             "clocks": clocks,
             "status_bits": int(np.bitwise_or.reduce(st)) if len(st) else 0,

@@ -244,6 +244,26 @@ __device__ __forceinline__ float tm_exp(float x)
     return (p * s1) * s2;
 }
 
+// e^x for -32 < x <= 0 (the start e^-m of the Poisson search): tm_exp's
+// arithmetic without its range checks and with one scale by 2^k.  On this range
+// k >= -47 and the scaled value is a normal float, so the single scale is
+// exact, as tm_exp's two half scales are: the same bits as tm_exp.
+__device__ __forceinline__ float tm_exp_neg_small(float x)
+{
+    const float k = rintf(x * 0x1.715476p+0f);
+    float r = fmaf(-k, 0x1.62ep-1f, x);
+    r = fmaf(-k, 0x1.0bfbe8p-15f, r);
+    float p = (float)(1.0 / 5040.0);
+    p = fmaf(r, p, (float)(1.0 / 720.0));
+    p = fmaf(r, p, (float)(1.0 / 120.0));
+    p = fmaf(r, p, (float)(1.0 / 24.0));
+    p = fmaf(r, p, (float)(1.0 / 6.0));
+    p = fmaf(r, p, 0.5f);
+    p = fmaf(r, p, 1.0f);
+    p = fmaf(r, p, 1.0f);
+    return p * __uint_as_float((uint32_t)((int)k + 127) << 23);
+}
+
 // 1 - e^-m for m >= 0 (alternating series below 0.25)
 __device__ __forceinline__ double tm_negexpm1(double m)
 {
@@ -587,26 +607,28 @@ __device__ __forceinline__ float dornic_draw_fast(uint64_t seed, uint32_t site, 
         const float u = (float)r.x * 0x1p-32f;
         // e^-m is only needed once u < q; below m = 0.25 q has its own series
         const bool small = m < 0.25f;
-        float p = small ? 0.0f : tm_exp(-m);
+        float p = small ? 0.0f : tm_exp_neg_small(-m);
         float q = small ? tm_negexpm1(m) : 1.0f - p;
-        if (small && u < q) p = tm_exp(-m);
+        if (small && u < q) p = tm_exp_neg_small(-m);
         // four terms per trip: the same products and differences as one term
-        // per trip (kFastInv is a multiple of 4), with a quarter of the loop
-        // control and the table loads issued together
+        // per trip (kFastInv is a multiple of 4), tested after the second and
+        // the fourth term.  q only decreases (p >= 0), so the terms with u < q
+        // form a prefix, and a failed test counts the one term before it that
+        // still had u < q -- the same count as testing every term, with half the
+        // branches.
         int it = 0;
         while (u < q && it < kFastInv) {
             const float4 r4 = *reinterpret_cast<const float4*>(tb.rcp + it + 1);
             const float p1 = (p * m) * r4.x;
             const float q1 = q - p1;
-            if (!(u < q1)) { it += 1; q = q1; break; }
             const float p2 = (p1 * m) * r4.y;
             const float q2 = q1 - p2;
-            if (!(u < q2)) { it += 2; q = q2; break; }
+            if (!(u < q2)) { it += 1 + (int)(u < q1); q = q2; break; }
             const float p3 = (p2 * m) * r4.z;
             const float q3 = q2 - p3;
-            if (!(u < q3)) { it += 3; q = q3; break; }
             p = (p3 * m) * r4.w;
             q = q3 - p;
+            if (!(u < q)) { it += 3 + (int)(u < q3); break; }
             it += 4;
         }
         if (u < q) { deferred = true; return 0.0f; }

@@ -16,6 +16,14 @@
 
 namespace tmg {
 
+// c + s * x for a power of two s: s * x is exact, so the fused form rounds once,
+// as the separate multiply and add do -- the same bits in one instruction.
+template <typename T>
+__device__ __forceinline__ T add_pow2_times(T c, T s, T x)
+{
+    return Tr<T>::fma_(s, x, c);
+}
+
 // Right-hand side at region cell c of S (f_2Dor, or f_2D when DET); R per instance.
 template <typename T, bool DET>
 __device__ __forceinline__ void rk_rhs_cell(const RK4Args<T>& A, const T* S, int c, T R, T& fP, T& fW, T& fO)
@@ -40,10 +48,10 @@ __device__ __forceinline__ void rk_rhs_cell(const RK4Args<T>& A, const T* S, int
         fP = ((A.cgmax * Wc) * Pc) * iwk;
         upt = upt_num * iwk;
     }
-    const T lapW = (((SW[cn] + SW[cs]) + SW[cw]) + SW[ce]) - T(4) * Wc;
-    const T lapO = (((SO[cn] + SO[cs]) + SO[cw]) + SO[ce]) - T(4) * Oc;
+    const T lapW = add_pow2_times(((SW[cn] + SW[cs]) + SW[cw]) + SW[ce], T(-4), Wc);
+    const T lapO = add_pow2_times(((SO[cn] + SO[cs]) + SO[cw]) + SO[ce], T(-4), Oc);
     if (DET) {
-        const T lapP = (((SP[cn] + SP[cs]) + SP[cw]) + SP[ce]) - T(4) * Pc;
+        const T lapP = add_pow2_times(((SP[cn] + SP[cs]) + SP[cw]) + SP[ce], T(-4), Pc);
         fP = (fP - A.d * Pc) + A.DPx * lapP;
     }
     fW = ((infil - upt) - A.rW * Wc) + A.DWx * lapW;
@@ -200,8 +208,9 @@ __global__ void __launch_bounds__(RK_THREADS, (sizeof(T) == 4 ? RK_CTAS : 1)) rk
                 } else if (s == 3) {
                     acc[0][j] = acc[0][j] + k0; acc[1][j] = acc[1][j] + k1; acc[2][j] = acc[2][j] + k2;
                 } else {
-                    acc[0][j] = acc[0][j] + T(2) * k0; acc[1][j] = acc[1][j] + T(2) * k1;
-                    acc[2][j] = acc[2][j] + T(2) * k2;
+                    acc[0][j] = add_pow2_times(acc[0][j], T(2), k0);
+                    acc[1][j] = add_pow2_times(acc[1][j], T(2), k1);
+                    acc[2][j] = add_pow2_times(acc[2][j], T(2), k2);
                 }
                 if (s < 3) {
                     D[c] = X0[c] + coef * k0;
@@ -295,12 +304,12 @@ __device__ __forceinline__ T dp_det_rhs(const DetTileArgs<T>& A, const T* S, int
     T f = (a * r) - ((A.b * r) * r);
     if (A.cubic) f = f - ((A.c * r) * r) * r;
     if constexpr (RAD == 1) {
-        const T lap = (((S[c - rx] + S[c + rx]) + S[c - 1]) + S[c + 1]) - T(4) * r;
+        const T lap = add_pow2_times(((S[c - rx] + S[c + rx]) + S[c - 1]) + S[c + 1], T(-4), r);
         f = f + A.dlap * lap;
     } else {
         const T o2 = ((S[c - 2 * rx] + S[c + 2 * rx]) + S[c - 2]) + S[c + 2];
         const T o1 = ((S[c - rx] + S[c + rx]) + S[c - 1]) + S[c + 1];
-        const T sm = (T(1) * o2 - T(16) * o1) + T(60) * r;
+        const T sm = add_pow2_times(o2, T(-16), o1) + T(60) * r;
         f = f - A.dk12 * sm;
     }
     return f;
@@ -352,7 +361,7 @@ __global__ void __launch_bounds__(RK_THREADS, 1) dp_det_tile_kernel(const DetTil
                 const T kv = dp_det_rhs<T, RAD>(A, S, c, RX, a);
                 if (s == 0) acc[j] = kv;
                 else if (s == NST - 1) acc[j] = acc[j] + kv;
-                else acc[j] = acc[j] + T(2) * kv;
+                else acc[j] = add_pow2_times(acc[j], T(2), kv);
                 if (s < NST - 1) D[c] = X0[c] + coef * kv;
             }
             if (s < NST - 1) {

@@ -65,7 +65,9 @@ __device__ __forceinline__ T finish_site(const DornicArgs<T>& A, T rs, T bi, uns
         const T k2 = rem_f(rs + A.dt2 * k1, bi, A.c, A.cubic);
         const T k3 = rem_f(rs + A.dt2 * k2, bi, A.c, A.cubic);
         const T k4 = rem_f(rs + A.dt * k3, bi, A.c, A.cubic);
-        res = rs + A.dt6 * (((k1 + T(2) * k2) + T(2) * k3) + k4);
+        // (k1 + 2 k2) + 2 k3: the doubling is exact, so each fused add rounds once as
+        // the separate multiply and add do (same bits, one instruction)
+        res = rs + A.dt6 * (Tr<T>::fma_(T(2), k3, Tr<T>::fma_(T(2), k2, k1)) + k4);
     } else {
         res = rs;
     }
