@@ -305,19 +305,29 @@ def late_regime(ctx, tmg, torch, args, burn=600, steps=10):
     b.enqueue_steps(burn)
     obs, _ = b.advance(0, [b.step])
     active = float(obs[0, :, 1].sum()) / (len(Ls) * 1024 * 1024)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with torch.cuda.stream(stream):
-        e0.record(stream)
-        for _ in range(steps):
-            b.enqueue_steps(1)
-        e1.record(stream)
-    e1.synchronize()
-    ms = e0.elapsed_time(e1) / steps
+    auto_form = b.get_draw_variant()[1]   # the search form the batch chose while burning in
+
+    def timed(n):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for _ in range(n):
+                b.enqueue_steps(1)
+            e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / n
+
+    ms = timed(steps)
+    per_form = {}
+    for form in (0, 1):
+        b.set_draw_variant(form + 1)
+        per_form[f"form{form}_ms_per_step"] = timed(steps)
     sites = len(Ls) * 1024 * 1024
     b.close()
     return {"burn_steps": burn, "t": burn * MODEL["dt"], "active_site_fraction": active, "ms_per_step": ms,
             "site_updates_per_s": sites / (ms * 1e-3),
-            "hbm_frac": BYTES_PER_SITE_FP32 * sites / (ms * 1e-3) / 1e9 / peaks()[0]}
+            "hbm_frac": BYTES_PER_SITE_FP32 * sites / (ms * 1e-3) / 1e9 / peaks()[0],
+            "search_form_chosen": auto_form, **per_form}
 
 
 def rietkerk_4096(ctx, tmg, torch, args, steps=10, L=4096, precision=None):

@@ -146,7 +146,11 @@ int64_t tm_batch_step(const tm_batch* b);                  /* steps taken so far
 
 /* State transfer; host_fields/dev_fields hold tm_batch_total_elems() elements of
  * the batch precision in the packed layout.  Upload resets the step counter to
- * `step` (the Philox counter of the next step) and revives extinct instances. */
+ * `step` (the Philox counter of the next step) and revives extinct instances.
+ * tm_batch_upload reads page-locked host memory (cudaHostAlloc, cudaHostRegister)
+ * with a copy kernel over the host link when the buffer starts on a 16-byte
+ * boundary, and other host memory through cudaMemcpyAsync; it returns after the
+ * copy and the check of the uploaded state. */
 int tm_batch_upload(tm_batch* b, const void* host_fields, int64_t step);
 int tm_batch_download(tm_batch* b, void* host_fields);
 int tm_batch_upload_device(tm_batch* b, const void* dev_fields, int64_t step);

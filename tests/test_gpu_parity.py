@@ -173,6 +173,34 @@ def test_search_forms_give_the_same_draws(tmg, oracle, ctx):
     b.close()
 
 
+def test_upload_paths_agree(tmg, ctx):
+    """Uploads from pageable memory (copy engines), from page-locked memory (copy kernel)
+    and from page-locked memory 4 bytes off a 16-byte boundary (copy engines) leave the
+    same state, and the check of the uploaded state runs on each."""
+    torch = pytest.importorskip("torch")
+    Ls = [64, 33, 100]
+    inst = tmg.instances(Ls, [1, 2, 3], 0.72)
+    b = tmg.Batch(ctx, tmg.dp_model(), inst, tmg.TM_FP32)
+    init = tmg.pack([f.astype(np.float32) for f in _init_fields(Ls, 4)], inst, 1, np.float32)
+    b.upload(init)
+    assert np.array_equal(b.download_packed(), init)
+    pinned = torch.empty(init.size + 1, dtype=torch.float32, pin_memory=True)
+    pn = pinned.numpy()
+    pn[:init.size] = init
+    b.upload(pn[:init.size])
+    assert np.array_equal(b.download_packed(), init)
+    pn[1:] = init
+    b.upload(pn[1:])
+    assert np.array_equal(b.download_packed(), init)
+    _, off, _ = tmg.layout(inst, 1)
+    pn[:init.size] = init
+    pn[off[1] + 5] = -1.0
+    b.upload(pn[:init.size])
+    _, st = b.advance(0, [])
+    assert st.tolist() == [0, tmg.TM_STATUS_NEGATIVE, 0]
+    b.close()
+
+
 def test_small_batch_gets_short_tasks(tmg, ctx):
     """A batch with too few 8-row tasks to fill the GPU starts with fewer rows per task
     (one 128^2 lattice: 64 tasks of 8 rows); a large batch keeps 8."""

@@ -727,7 +727,18 @@ int tm_batch_upload(tm_batch* b, const void* host, int64_t step)
 {
     if (!b || !host || step < 0) return TM_ERR_INVALID;
     TM_CUDA(cudaSetDevice(b->ctx->device));
-    TM_CUDA(cudaMemcpyAsync(b->buf[b->cur], host, (size_t)b->total * b->esize, cudaMemcpyHostToDevice, b->ctx->stream));
+    const size_t bytes = (size_t)b->total * b->esize;
+    // page-locked host memory mapped into the device's address space: read by a copy
+    // kernel; any other host memory: through the copy engines
+    const void* mapped = nullptr;
+    cudaPointerAttributes pa{};
+    if (cudaPointerGetAttributes(&pa, host) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer)
+        mapped = pa.devicePointer;
+    (void)cudaGetLastError();
+    if (mapped && ((uintptr_t)mapped & 15u) == 0 && (bytes & 15u) == 0)
+        TM_CUDA(launch_copy_in(mapped, b->buf[b->cur], bytes, b->ctx->num_sms * 4, b->ctx->stream));
+    else
+        TM_CUDA(cudaMemcpyAsync(b->buf[b->cur], host, bytes, cudaMemcpyHostToDevice, b->ctx->stream));
     return reset_after_upload(b, step);
 }
 

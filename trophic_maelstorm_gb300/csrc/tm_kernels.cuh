@@ -100,6 +100,7 @@ cudaError_t launch_finalize(const double* partial, const int* task_begin, const 
 cudaError_t launch_consts(const double* a0, const double* astep, int n, double diff4, double sigma2, double dt,
                           const long long* step_base, long long step_off, Dc4* out, cudaStream_t s);
 cudaError_t launch_set_step(long long* d_step, long long v, cudaStream_t s);
+cudaError_t launch_copy_in(const void* src, void* dst, size_t bytes, int grid, cudaStream_t s);
 template <typename T>
 cudaError_t launch_box_means(const T* field, int L, int box, double* out, cudaStream_t s);
 template <typename T>

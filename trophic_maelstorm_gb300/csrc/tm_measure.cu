@@ -197,6 +197,25 @@ template cudaError_t launch_validate<float>(const float*, const InstTables&, con
 template cudaError_t launch_validate<double>(const double*, const InstTables&, const int4*, int, int, int,
                                              cudaStream_t);
 
+// Upload of a state from page-locked host memory: the device reads it over the host
+// link, 16 bytes per load, grid-stride.  On GB300 machines the copy engines' host-to-device
+// rate dropped from 211 to 18-30 GB/s in some copies after compute phases, while these
+// loads of the same buffer held 212 GB/s.
+__global__ void __launch_bounds__(512) copy_in_kernel(const uint4* __restrict__ src, uint4* __restrict__ dst,
+                                                      long long n16)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += stride) dst[i] = src[i];
+}
+
+cudaError_t launch_copy_in(const void* src, void* dst, size_t bytes, int grid, cudaStream_t s)
+{
+    if (bytes == 0) return cudaSuccess;
+    if (((uintptr_t)src | (uintptr_t)dst | (uintptr_t)bytes) & 15u) return cudaErrorInvalidValue;
+    copy_in_kernel<<<grid, 512, 0, s>>>((const uint4*)src, (uint4*)dst, (long long)(bytes / 16));
+    return cudaGetLastError();
+}
+
 // One warp per instance: obs_row[k*W + f], W = 2 (DP: mean, active), 3 (DP
 // spreading: mean, active, summed squared distance) or 4 (Rietkerk: mean P, W, O,
 // active P).  With dp_extinction, an instance seen with no active site is marked
