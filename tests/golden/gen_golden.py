@@ -38,6 +38,13 @@ ref_libstdcxx.npz  draws of the libstdc++ poisson_distribution / gamma_distribut
     python tests/golden/gen_golden.py --lnspace    # only ref_lnspace.npz
     python tests/golden/gen_golden.py --fke        # only ref_fke.npz
     python tests/golden/gen_golden.py --libstdcxx  # only ref_libstdcxx.npz
+    python tests/golden/gen_golden.py --rk-ensemble  # only ref_rk_ensemble.npz
+
+ref_rk_ensemble.npz  replicates of the reference's stochastic Rietkerk step (P-Dornic loop
+                   with libstdc++ draws from one seeded std::mt19937_64 per replicate, the
+                   reference's compiled RK4_Integrate_Stochastic_1Sp, the clamp) on one
+                   16^2 start: per replicate the final mean P, W, O, the occupied P sites
+                   and P at two sites, compared statistically with the GPU's ensemble.
 """
 from __future__ import annotations
 
@@ -83,6 +90,7 @@ def load(names=("dp", "rietkerk", "multisp")):
     r = libs["rietkerk"]
     r.ref_rk_det_steps.argtypes = [dp, C.c_int, C.c_int] + [C.c_double] * 14
     r.ref_rk_stoch_remainder.argtypes = [dp, C.c_int] + [C.c_double] * 12
+    r.ref_rk_stoch_steps.argtypes = [dp, C.c_int, C.c_int, C.c_ulonglong] + [C.c_double] * 16
     libs["multisp"].ref_ms_rk4_remainder.argtypes = [dp, C.c_int, C.c_double, C.c_double, C.c_double]
     cs = C.c_char_p
     libs["multisp"].ref_save_frame.argtypes = [dp, C.c_int, cs, cs, C.c_double, C.c_int, cs]
@@ -309,7 +317,43 @@ def libstdcxx(libs):
     return out
 
 
+# the Rietkerk ensemble case: 16^2, R = 1.0, sigma = 0.5, dt = 1e-3, 500 steps, 400 replicates;
+# P ~ U(0,1) with a bare 4 x 4 patch (its edge sites draw with Poisson mean 0) and a 4 x 4 patch
+# at P = 2e-3 (Poisson means near 16: the exact Poisson and Gamma branches)
+RK_ENS = dict(L=16, R=1.0, sigma=0.5, dt=1e-3, steps=500, n_rep=400, seed0=1000, eps=1e-10,
+              site_a=(10, 10), site_b=(5, 12))
+
+
+def rk_ensemble_start(rng):
+    L = RK_ENS["L"]
+    P = rng.uniform(0, 1, (L, L))
+    P[0:4, 0:4] = 0.0
+    P[8:12, 8:12] = 2e-3
+    return np.stack([P, np.full((L, L), 0.5), np.ones((L, L))])
+
+
+def rk_ensemble(libs):
+    e = RK_ENS
+    L = e["L"]
+    f0 = rk_ensemble_start(np.random.default_rng(77))
+    rows = []
+    for j in range(e["n_rep"]):
+        f = np.ascontiguousarray(f0.reshape(-1).copy())
+        libs["rietkerk"].ref_rk_stoch_steps(_p(f), L, e["steps"], e["seed0"] + j, e["R"], RK["c"], RK["gmax"],
+                                            RK["alpha"], RK["d"], RK["rW"], RK["W0"], RK["DP"], RK["DW"], RK["DO"],
+                                            RK["k1"], RK["k2"], e["sigma"], e["dt"], 1.0, e["eps"])
+        g = f.reshape(3, L, L)
+        rows.append([g[0].mean(), g[1].mean(), g[2].mean(), float((g[0] > 0).sum()), g[0][e["site_a"]],
+                     g[0][e["site_b"]]])
+    np.savez_compressed(os.path.join(HERE, "ref_rk_ensemble.npz"), start=f0, rows=np.array(rows),
+                        columns=np.array(["mean_P", "mean_W", "mean_O", "occupied_P", "P_site_a", "P_site_b"]),
+                        meta=np.array([L, e["R"], e["sigma"], e["dt"], e["steps"], e["n_rep"], e["seed0"], e["eps"]]))
+
+
 def main():
+    if "--rk-ensemble" in sys.argv:
+        rk_ensemble(load(("dp", "rietkerk", "multisp")))
+        return
     if "--libstdcxx" in sys.argv:
         np.savez_compressed(os.path.join(HERE, "ref_libstdcxx.npz"), **libstdcxx(load(("dp",))))
         return
@@ -327,6 +371,7 @@ def main():
     subprocess.run([sys.executable, os.path.abspath(__file__), "--fke"], check=True)
     subprocess.run([sys.executable, os.path.abspath(__file__), "--spectrum"], check=True)
     subprocess.run([sys.executable, os.path.abspath(__file__), "--lnspace"], check=True)
+    subprocess.run([sys.executable, os.path.abspath(__file__), "--rk-ensemble"], check=True)
     libs = load()
     rng = np.random.default_rng(20261203)
     np.savez_compressed(os.path.join(HERE, "ref_pins.npz"), **pins(libs, rng))

@@ -238,6 +238,27 @@ def test_rietkerk_matches_oracle(tmg, oracle, ctx, precision, sampler):
     b.close()
 
 
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32"])
+def test_rietkerk_ensemble_matches_reference(tmg, ctx, golden, precision):
+    """The GPU's stochastic Rietkerk step against replicates of the reference's step (its
+    P-Dornic loop with libstdc++ draws, its compiled remainder RK4, the clamp): 400
+    replicates of 500 steps, one batch; final mean P, W, O, occupied sites, two sites."""
+    from conftest import rk_ensemble_rows, assert_same_ensemble
+    g = golden["rk_ens"]
+    L, R, sigma, dt, steps, n_rep, _, eps = g["meta"]
+    L, steps, n_rep = int(L), int(steps), int(n_rep)
+    dtype = np.float64 if precision == 0 else np.float32
+    model = tmg.rietkerk_model(sigma=sigma, dt=dt, clamp_eps=eps)
+    inst = tmg.instances([L] * n_rep, list(range(n_rep)), R)
+    b = tmg.Batch(ctx, model, inst, precision)
+    b.upload([g["start"].astype(dtype)] * n_rep)
+    _, st = b.advance(steps, [steps])
+    assert not st.any()
+    fins = b.download()
+    b.close()
+    assert_same_ensemble(rk_ensemble_rows(fins), g["rows"], g["columns"])
+
+
 def test_rietkerk_noise_off_matches_reference(tmg, ctx, golden):
     """Noise-off Rietkerk RK4 (f_2D / RK4_Integrate) on the GPU against the reference's
     own output, to 1e-10 relative (the noise-off parity bar)."""
