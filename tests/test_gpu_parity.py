@@ -354,25 +354,37 @@ def test_reproducible_per_seed(tmg, ctx):
     assert np.array_equal(fin[256 * 256:], outs[0][1][256 * 256:])
 
 
-def test_gpu_ensemble_matches_reference(tmg, ctx, golden):
-    """percolation_dornic_2d on the GPU (1500 replicates in one batch) against the
-    reference's ensemble: rho(t) within 3.5 combined SE and KS p > 0.01/n_t."""
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32"])
+@pytest.mark.parametrize("tag,n_rep", [("crit", 1500), ("active", 400), ("site", 3000)])
+def test_gpu_ensemble_matches_reference(tmg, ctx, golden, tag, n_rep, precision):
+    """percolation_dornic_2d on the GPU (every replicate in one batch) against the
+    reference's ensembles at L = 8 near the absorbing transition, L = 8 active and a single
+    site: rho(t) and survival within 3.5 combined standard errors, and the distribution of
+    rho(t) over replicates by two-sample KS, p > 0.01 / n_t at every time."""
     from scipy import stats
     ens = golden["ens"]
-    L, a, b, D, sig, dt, dx = ens["crit_meta"]
-    t = ens["crit_t"]
+    L, a, b, D, sig, dt, dx = ens[f"{tag}_meta"]
+    t = ens[f"{tag}_t"]
     steps = np.rint(t / dt).astype(np.int64)
-    r = 1500
-    inst = tmg.instances([int(L)] * r, range(5000, 5000 + r), a)
+    dtype = np.float64 if precision == 0 else np.float32
+    inst = tmg.instances([int(L)] * n_rep, range(5000, 5000 + n_rep), a)
     model = tmg.dp_model(b=b, D=D, sigma=sig, dt=dt, dx=dx)
-    init = tmg.pack([ens["crit_rho0"]] * r, inst, 1, np.float64)
-    obs, st, _ = tmg.run_dp(ctx, model, inst, init, int(steps[-1]), steps, tmg.TM_FP64)
-    M = obs[:, :, 0].T
-    R = ens["crit_mean"]
-    for j in range(1, len(t)):
-        se = np.sqrt(M[:, j].var() / r + R[:, j].var() / len(R))
-        assert abs(M[:, j].mean() - R[:, j].mean()) < 3.5 * se
-        assert stats.ks_2samp(M[:, j], R[:, j]).pvalue > 0.01 / len(t)
+    init = tmg.pack([ens[f"{tag}_rho0"]] * n_rep, inst, 1, dtype)
+    obs, st, _ = tmg.run_dp(ctx, model, inst, init, int(steps[-1]), steps, precision)
+    assert not st.any()
+    M, A = obs[:, :, 0].T, obs[:, :, 1].T
+    R, RA = ens[f"{tag}_mean"], ens[f"{tag}_active"]
+    n_t = len(t)
+    for j in range(1, n_t):
+        se = np.sqrt(M[:, j].var() / len(M) + R[:, j].var() / len(R))
+        if se > 0:
+            assert abs(M[:, j].mean() - R[:, j].mean()) < 3.5 * se, (tag, j)
+        ps, pr = (A[:, j] > 0).mean(), (RA[:, j] > 0).mean()
+        se_s = np.sqrt(ps * (1 - ps) / len(A) + pr * (1 - pr) / len(RA))
+        if se_s > 0:
+            assert abs(ps - pr) < 3.5 * se_s, (tag, j)
+        if M[:, j].std() > 0 and R[:, j].std() > 0:
+            assert stats.ks_2samp(M[:, j], R[:, j]).pvalue > 0.01 / n_t, (tag, j)
 
 
 def test_reference_rows_shape(tmg, ctx):
