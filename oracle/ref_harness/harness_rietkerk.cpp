@@ -67,7 +67,7 @@ void ref_rk_det_steps(double* f, int g, int n_steps, double R, double c, double 
 // n_steps of the reference's stochastic Rietkerk step on f = [P|W|O], in place, for
 // one replicate: the P-Dornic loop of rietkerk_DorFPE_2D_MultiSp
 // (rietkerk_bjork_FKE.cpp:4155-4195: skip, Poisson above/below 100, Gamma above/below
-// 100, with the constants of :3846-3849) restated here -- the driver around it
+// 100, with the constants of :3846-3849) restated here -- the simulation function around it
 // cannot run without exprtk -- with the reference's libstdc++ distributions and one
 // std::mt19937_64 per replicate; then the reference's own compiled
 // RK4_Integrate_Stochastic_1Sp (:2393) for the remainder; then the clamp and the
