@@ -65,6 +65,8 @@ struct ColSum<float> {
 // spread (DP), f = 1 is the sum over occupied sites of the squared distance
 // (row - cy)^2 + (col - cx)^2 from the seed site (meansq_spread_of_vector,
 // stochasticSPDP.cpp:156-170), summed as integers; cx, cy < 0 mean L/2.
+constexpr int kChunk = 8;   // rows whose loads a warp issues together
+
 template <typename T>
 __global__ void __launch_bounds__(256) measure_kernel(const T* state, const InstTables it, const int4* tasks,
                                                       int n_tasks, int nf, double* partial, int spread, int scx,
@@ -87,18 +89,31 @@ __global__ void __launch_bounds__(256) measure_kernel(const T* state, const Inst
             const long long fs = it.fstride[k];
             const bool in = x < L;
             const long long cx = scx < 0 ? L / 2 : scx, cy = scy < 0 ? L / 2 : scy;
-            for (int r = 0; r < tk.w; ++r) {
-                const long long i = (long long)(tk.z + r) * L + x;
-                const T v = in ? base[i] : T(0);
-                c0.add(v);
-                ac += __popc(__ballot_sync(0xffffffffu, v > T(0)));
-                if (spread && v > T(0)) {
-                    const long long dy = (long long)(tk.z + r) - cy, dx = (long long)x - cx;
-                    sq += dy * dy + dx * dx;
+            // rows in chunks of kChunk: every load of a chunk is issued before the
+            // sums use them (the state streams from HBM once; the sums keep row order)
+            for (int r0 = 0; r0 < tk.w; r0 += kChunk) {
+                T v0[kChunk], v1[kChunk], v2[kChunk];
+#pragma unroll
+                for (int j = 0; j < kChunk; ++j) {
+                    const bool ok = in && r0 + j < tk.w;
+                    const long long i = (long long)(tk.z + r0 + j) * L + x;
+                    v0[j] = ok ? base[i] : T(0);
+                    v1[j] = (nf == 3 && ok) ? base[i + fs] : T(0);
+                    v2[j] = (nf == 3 && ok) ? base[i + 2 * fs] : T(0);
                 }
-                if (nf == 3 && in) {
-                    c1.add(base[i + fs]);
-                    c2.add(base[i + 2 * fs]);
+#pragma unroll
+                for (int j = 0; j < kChunk; ++j) {
+                    if (r0 + j >= tk.w) break;
+                    c0.add(v0[j]);
+                    ac += __popc(__ballot_sync(0xffffffffu, v0[j] > T(0)));
+                    if (spread && v0[j] > T(0)) {
+                        const long long dy = (long long)(tk.z + r0 + j) - cy, dx = (long long)x - cx;
+                        sq += dy * dy + dx * dx;
+                    }
+                    if (nf == 3 && in) {
+                        c1.add(v1[j]);
+                        c2.add(v2[j]);
+                    }
                 }
             }
         }
@@ -177,8 +192,15 @@ __global__ void __launch_bounds__(256) validate_kernel(const T* state, const Ins
         if (x < L) {
             const T* base = state + it.off[k];
             const long long fs = it.fstride[k];
-            for (int r = 0; r < tk.w; ++r)
-                for (int f = 0; f < nf; ++f) st |= value_status(base[f * fs + (long long)(tk.z + r) * L + x]);
+            for (int f = 0; f < nf; ++f)
+                for (int r0 = 0; r0 < tk.w; r0 += kChunk) {
+                    T v[kChunk];
+#pragma unroll
+                    for (int j = 0; j < kChunk; ++j)
+                        v[j] = r0 + j < tk.w ? base[f * fs + (long long)(tk.z + r0 + j) * L + x] : T(0);
+#pragma unroll
+                    for (int j = 0; j < kChunk; ++j) st |= value_status(v[j]);
+                }
         }
         st = __reduce_or_sync(0xffffffffu, st);
         if (lane == 0 && st) atomicOr(it.status + k, st);
