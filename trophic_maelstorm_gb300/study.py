@@ -384,6 +384,7 @@ def main():
         return
     if a.pattern:
         print(json.dumps(rietkerk_pattern_precision(a.L if a.L != 4096 else 256, a.R if a.R != 0.9 else 1.2,
+                                                    reps=a.reps if a.reps != 64 else 4,
                                                     steps=a.steps if a.steps != 20000 else 500000)))
         return
     if a.sweep_run:
