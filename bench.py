@@ -56,7 +56,7 @@ def a_values():
 
 def workload(kind="sweep"):
     Ls, seeds, avs = [], [], []
-    if kind == "l1024x64":  # profiling case: 64 instances of the L=1024 subset (268 MB per state buffer)
+    if kind in ("l1024x64", "l1024x64_dilute"):  # profiling cases: 64 instances of the L=1024 subset (268 MB per buffer)
         for r in range(64):
             Ls.append(1024); seeds.append(1_000_003 * r + 17); avs.append(float(a_values()[r % NA]))
         return Ls, seeds, avs
@@ -197,8 +197,9 @@ def workload_config(kind):
             if kind == "sweep" else f"profiling case {kind}",
             "sites_per_step": int(sum(L * L for L in workload(kind)[0])), "b": 2.0, "D": 1.0, "sigma": 1.0,
             "dt": 0.1, "a_values": f"16 log-spaced in [{a_values()[0]:.4f}, {a_values()[-1]:.4f}]",
-            "init": "1+U(-0.01,0.01), all sites live", "state": "FP32, FP64 reductions",
-            "l2": "inputs larger than L2 (2.86 GB state per buffer)"}
+            "init": "half the sites U(0, 0.5), the others 0" if kind == "l1024x64_dilute"
+            else "1+U(-0.01,0.01), all sites live", "state": "FP32, FP64 reductions",
+            "l2": f"inputs larger than L2 ({4 * sum(L * L for L in workload(kind)[0]) / 1e9:.2f} GB state per buffer)"}
 
 
 def run_reference(args):
@@ -486,7 +487,13 @@ def run_ours(args):
     hv[:] = 0
     _, off, fs = tmg.layout(inst, 1)
     for k, L in enumerate(Ls):
-        hv[off[k]: off[k] + L * L] = rng.uniform(-0.01, 0.01, L * L).astype(np.float32) + np.float32(1.0)
+        if args.workload == "l1024x64_dilute":   # a dilute lattice: half the sites empty, the rest U(0, 0.5)
+            v = rng.uniform(0.0, 0.5, L * L).astype(np.float32)
+            v[rng.random(L * L) < 0.5] = 0.0
+            hv[off[k]: off[k] + L * L] = v
+        else:
+            hv[off[k]: off[k] + L * L] = rng.uniform(-0.01, 0.01, L * L).astype(np.float32) + np.float32(1.0)
+    b.set_draw_variant(args.draw_variant)
     b.upload(hv)
 
     if args.autotune:
@@ -610,7 +617,9 @@ def main():
                     help="skip the launch-shape autotuner (it runs before the timed region)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
-    ap.add_argument("--workload", default="sweep", choices=["sweep", "l1024x64"])
+    ap.add_argument("--workload", default="sweep", choices=["sweep", "l1024x64", "l1024x64_dilute"])
+    ap.add_argument("--draw-variant", type=int, default=0, choices=[0, 1, 2],
+                    help="form of the FP32 Poisson search: 0 chosen by timing, 1 or 2 fixed (same draws)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
     args = ap.parse_args()
