@@ -21,6 +21,10 @@ Metric: site-updates/s (one lattice site of one instance advanced one step).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
+Profiling cases (not the metric): --workload l1024x64 (64 x 1024^2, fully active) and
+l1024x64_dilute (half the sites empty); --draw-variant 1|2 fixes the form of the FP32
+Poisson search (0, the default, lets the batch choose by timing; the draws are the same).
+
 --impl reference times the CPU restatement of the reference's step (the
 oracle, OpenMP over instances, all host threads) on a bounded sample of the
 same workload: the reference's sources are not on the benchmark machine.
