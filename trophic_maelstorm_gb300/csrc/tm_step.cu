@@ -51,6 +51,13 @@ __host__ __device__ __forceinline__ size_t warp_scratch_bytes(int rows_cap)
 }
 
 __device__ __forceinline__ bool is_pos_zero(float x) { return __float_as_uint(x) == 0u; }
+
+// Row-major site index y L + x, the Philox counter's site word: unsigned, so it is
+// defined for every L the batches accept (L <= 65535 keeps L^2 below 2^32).
+__device__ __forceinline__ uint32_t site_index(int y, int L, int x)
+{
+    return (uint32_t)y * (uint32_t)L + (uint32_t)x;
+}
 __device__ __forceinline__ bool is_pos_zero(double x) { return __double_as_longlong(x) == 0LL; }
 
 // Remainder, clamp and status bits of one site after its Dornic draw.
@@ -207,8 +214,8 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
                     bool deferred = false;
                     if (has) {
                         const int li = Wqi[j];
-                        const int site = (y0 + (li >> 5)) * L + x0 + (li & 31);
-                        const float v = dornic_draw_fast<INV>(seed, (uint32_t)site, step, Wqm[j], Wqmu[j],
+                        const uint32_t site = site_index(y0 + (li >> 5), L, x0 + (li & 31));
+                        const float v = dornic_draw_fast<INV>(seed, site, step, Wqm[j], Wqmu[j],
                                                               inv_lambda, SAMP, tab, deferred);
                         if (deferred) atomicOr(Wrows + (li & 31), 1u << (li >> 5));
                         else Wres[li] = v;
@@ -218,7 +225,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
                     if (has && deferred) {
                         const int li = Wqi[j];
                         A.dlist[(long long)gw * A.seg_cap + nseg + __popc(bal & lt_mask)] =
-                            make_uint4((unsigned)k, (unsigned)((y0 + (li >> 5)) * L + x0 + (li & 31)),
+                            make_uint4((unsigned)k, site_index(y0 + (li >> 5), L, x0 + (li & 31)),
                                        __float_as_uint(Wqm[j]), __float_as_uint(Wqmu[j]));
                     }
                     nseg += __popc(bal);
@@ -276,7 +283,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
                 } else {
                     const int j = Wdef[e - nc];
                     const int li = Wqi[j];
-                    se = (uint32_t)((y0 + (li >> 5)) * L + x0 + (li & 31));
+                    se = site_index(y0 + (li >> 5), L, x0 + (li & 31));
                     me = Wqm[j];
                     mue = Wqmu[j];
                 }
@@ -291,7 +298,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
             const int j = Wdef[lim + lane - nc];
             const int li = Wqi[j];
             Ck[lane] = k;
-            Cs[lane] = (uint32_t)((y0 + (li >> 5)) * L + x0 + (li & 31));
+            Cs[lane] = site_index(y0 + (li >> 5), L, x0 + (li & 31));
             Cm[lane] = Wqm[j];
             Cmu[lane] = Wqmu[j];
         }
