@@ -239,9 +239,9 @@ def run_reference(args):
                                    "fully active start, FP32 port, OpenMP over instances",
                          "fp64_port_value": val64,
                          "fp64_port_sample": f"the same sample in FP64 (the reference's arithmetic), {n64} steps",
-                         "calibration": "on one x86 core the FP32 port runs at 1.03x the reference's own "
-                                        "percolationDornic_2D at its production flags and the FP64 port at 0.81x "
-                                        "(profiles/cpu_reference_vs_port.md)"},
+                         "calibration": "on x86 the FP32 port runs at 1.00x (one core) and 1.17x (eight cores, one "
+                                        "a per thread) the reference's own percolationDornic_2D at its production "
+                                        "flags (profiles/cpu_reference_vs_port.md)"},
         "e2e": {"value": val, "unit": "site-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

@@ -8,6 +8,7 @@
 #include <iostream>
 #include <sstream>
 #include <cstring>
+#include <omp.h>
 using std::vector;
 
 void percolationDornic_2D(vector<vector<double>>& Rho, vector<double>& t_meas, double Rh0[], double t_max,
@@ -23,6 +24,11 @@ struct Mute {  // the reference prints progress to std::cout; keep it quiet
     std::ostringstream sink;
     Mute() : old(std::cout.rdbuf(sink.rdbuf())) {}
     ~Mute() { std::cout.rdbuf(old); }
+};
+// a stream buffer that drops everything and keeps no state, so threads may share it
+struct NullBuf : std::streambuf {
+    int overflow(int c) override { return c; }
+    std::streamsize xsputn(const char*, std::streamsize n) override { return n; }
 };
 }
 
@@ -45,6 +51,28 @@ int ref_percolation_dornic(const double* t_meas, int n_meas, const double* rho0,
         ++n;
     }
     return n;
+}
+
+// The reference's parallel model (critical_exp_delta, stochasticSPDP.cpp:1343-1369):
+// one OpenMP thread per value of a, each running percolationDornic_2D (r = 1) from
+// the same start.  Returns the wall time in seconds.
+double ref_percolation_dornic_par(const double* t_meas, int n_meas, const double* rho0, double t_max, const double* a,
+                                  int n_a, double b, double D, double sigma, double dt, double dx, int g, int threads)
+{
+    NullBuf null;
+    std::streambuf* old = std::cout.rdbuf(&null);
+    const vector<double> tm(t_meas, t_meas + n_meas);
+    const double t0 = omp_get_wtime();
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 1)
+    for (int i = 0; i < n_a; ++i) {
+        vector<vector<double>> out;
+        vector<double> tmi = tm;
+        vector<double> r0(rho0, rho0 + (size_t)g * g);
+        percolationDornic_2D(out, tmi, r0.data(), t_max, a[i], b, D, sigma, dt, dx, 1, g);
+    }
+    const double sec = omp_get_wtime() - t0;
+    std::cout.rdbuf(old);
+    return sec;
 }
 
 // percNoDiff_2D: noise-off RK4 with the 4th-order cross Laplacian.  Frames at the
