@@ -404,10 +404,8 @@ int run_steps(tm_batch* b, int64_t n)
                 if (k == 1) form = 1 - b->draw_cur;
                 if (k >= 0 && k <= 2) {
                     sl = &b->ab[k];
-                    if (!sl->e0) {
-                        TM_CUDA(cudaEventCreate(&sl->e0));
-                        TM_CUDA(cudaEventCreate(&sl->e1));
-                    }
+                    if (!sl->e0) TM_CUDA(cudaEventCreate(&sl->e0));
+                    if (!sl->e1) TM_CUDA(cudaEventCreate(&sl->e1));
                     sl->replay = r;
                     sl->form = form;
                 }
