@@ -168,8 +168,15 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
             T cur = act ? src[(long long)y0 * L + x] : T(0);
             T south = act ? src[(long long)((y0 == L - 1) ? 0 : y0 + 1) * L + x] : T(0);
             int nq = 0;
-            unsigned drows = 0;  // rows of this lane's column left to the general sampler
-            Wrows[lane] = 0u;
+            unsigned drows = 0;  // rows of this lane's column left to the general sampler (FP64)
+            unsigned st = 0;
+            // The FP32 DP step finishes and stores every site where its value is known:
+            // absorbing and noise-off sites in pass 1, drawn sites in pass 2, so it has no
+            // pass 3 and no round trip of the draws through shared memory.  (For P* of the
+            // Rietkerk step the compiler then spills; it keeps the three passes.)
+            constexpr bool kStoreEarly = sizeof(T) == 4 && REM != 2;
+            const T* __restrict__ sb = (kStoreEarly && A.site_b) ? A.site_b + A.it.off[k] : nullptr;
+            if (!kStoreEarly) Wrows[lane] = 0u;
             for (int r = 0; r < rows; ++r) {
                 const int y = y0 + r;
                 T next = T(0);
@@ -189,7 +196,20 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
                 const T alpha = A.dcoef * nsum;
                 const bool live = act && !(alpha == T(0) && cur == T(0)) && SAMP != 2;
                 const unsigned bal = __ballot_sync(0xffffffffu, live);
-                if (!live) Wres[r * 32 + lane] = (SAMP == 2 && act) ? a1 * cur + a2 * alpha : T(0);
+                if (!live) {
+                    if constexpr (kStoreEarly) {
+                        if (act) {
+                            const T rs = (SAMP == 2) ? a1 * cur + a2 * alpha : T(0);
+                            const long long o = (long long)y * L + x;
+                            T res = rs;
+                            if (!(A.zero_fixed && is_pos_zero(rs)))
+                                res = finish_site<T, REM>(A, rs, sb ? sb[o] : A.b, st);
+                            dst[o] = res;
+                        }
+                    } else {
+                        Wres[r * 32 + lane] = (SAMP == 2 && act) ? a1 * cur + a2 * alpha : T(0);
+                    }
+                }
                 if (sizeof(T) == 8 && live) drows |= 1u << r;
                 if (live) {
                     const int pos = nq + __popc(bal & lt_mask);
@@ -217,8 +237,18 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
                         const uint32_t site = site_index(y0 + (li >> 5), L, x0 + (li & 31));
                         const float v = dornic_draw_fast<INV>(seed, site, step, Wqm[j], Wqmu[j],
                                                               inv_lambda, SAMP, tab, deferred);
-                        if (deferred) atomicOr(Wrows + (li & 31), 1u << (li >> 5));
-                        else Wres[li] = v;
+                        if constexpr (kStoreEarly) {
+                            if (!deferred) {
+                                const long long o = (long long)(y0 + (li >> 5)) * L + x0 + (li & 31);
+                                T res = v;
+                                if (!(A.zero_fixed && is_pos_zero(v)))
+                                    res = finish_site<T, REM>(A, v, sb ? sb[o] : A.b, st);
+                                dst[o] = res;
+                            }
+                        } else {
+                            if (deferred) atomicOr(Wrows + (li & 31), 1u << (li >> 5));
+                            else Wres[li] = v;
+                        }
                     }
                     // deferred sites: appended to this warp's segment of the list
                     const unsigned bal = __ballot_sync(0xffffffffu, has && deferred);
@@ -231,7 +261,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
                     nseg += __popc(bal);
                 }
                 __syncwarp();
-                drows = Wrows[lane];
+                if constexpr (!kStoreEarly) drows = Wrows[lane];
             } else {
                 for (int j = lane; j < nq; j += 32) Wdef[j] = (unsigned short)j;
                 ndef = nq;
@@ -240,15 +270,14 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
             // pass 3: remainder, clamp, store (sites left to the general sampler
             // are finished and stored by it).  When zero_fixed holds a +0 draw --
             // every absorbing site -- finishes as +0 and skips the arithmetic.
-            unsigned st = 0;
-            if (act) {
-                const T* __restrict__ sb = A.site_b ? A.site_b + A.it.off[k] : nullptr;
+            if (act && !kStoreEarly) {
+                const T* __restrict__ sb3 = A.site_b ? A.site_b + A.it.off[k] : nullptr;
                 for (int r = 0; r < rows; ++r) {
                     if ((drows >> r) & 1u) continue;
                     const T rs = Wres[r * 32 + lane];
                     T res = rs;
                     if (!(A.zero_fixed && is_pos_zero(rs))) {
-                        const T bi = sb ? sb[(long long)(y0 + r) * L + x] : A.b;
+                        const T bi = sb3 ? sb3[(long long)(y0 + r) * L + x] : A.b;
                         res = finish_site<T, REM>(A, rs, bi, st);
                     }
                     dst[(long long)(y0 + r) * L + x] = res;
