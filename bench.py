@@ -22,8 +22,7 @@ Metric: site-updates/s (one lattice site of one instance advanced one step).
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 Profiling cases (not the metric): --workload l1024x64 (64 x 1024^2, fully active) and
-l1024x64_dilute (half the sites empty); --draw-variant 1|2 fixes the form of the FP32
-Poisson search (0, the default, lets the batch choose by timing; the draws are the same).
+l1024x64_dilute (half the sites empty).
 
 --impl reference times the CPU restatement of the reference's step (the
 oracle, OpenMP over instances, all host threads) on a bounded sample of the
@@ -310,7 +309,6 @@ def late_regime(ctx, tmg, torch, args, burn=600, steps=10):
     b.enqueue_steps(burn)
     obs, _ = b.advance(0, [b.step])
     active = float(obs[0, :, 1].sum()) / (len(Ls) * 1024 * 1024)
-    auto_form = b.get_draw_variant()[1]   # the search form the batch chose while burning in
 
     def timed(n):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -323,16 +321,11 @@ def late_regime(ctx, tmg, torch, args, burn=600, steps=10):
         return e0.elapsed_time(e1) / n
 
     ms = timed(steps)
-    per_form = {}
-    for form in (0, 1):
-        b.set_draw_variant(form + 1)
-        per_form[f"form{form}_ms_per_step"] = timed(steps)
     sites = len(Ls) * 1024 * 1024
     b.close()
     return {"burn_steps": burn, "t": burn * MODEL["dt"], "active_site_fraction": active, "ms_per_step": ms,
             "site_updates_per_s": sites / (ms * 1e-3),
-            "hbm_frac": BYTES_PER_SITE_FP32 * sites / (ms * 1e-3) / 1e9 / peaks()[0],
-            "search_form_chosen": auto_form, **per_form}
+            "hbm_frac": BYTES_PER_SITE_FP32 * sites / (ms * 1e-3) / 1e9 / peaks()[0]}
 
 
 def rietkerk_4096(ctx, tmg, torch, args, steps=10, L=4096, precision=None):
@@ -497,7 +490,6 @@ def run_ours(args):
             hv[off[k]: off[k] + L * L] = v
         else:
             hv[off[k]: off[k] + L * L] = rng.uniform(-0.01, 0.01, L * L).astype(np.float32) + np.float32(1.0)
-    b.set_draw_variant(args.draw_variant)
     b.upload(hv)
 
     if args.autotune:
@@ -622,8 +614,6 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--workload", default="sweep", choices=["sweep", "l1024x64", "l1024x64_dilute"])
-    ap.add_argument("--draw-variant", type=int, default=0, choices=[0, 1, 2],
-                    help="form of the FP32 Poisson search: 0 chosen by timing, 1 or 2 fixed (same draws)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
     args = ap.parse_args()

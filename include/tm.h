@@ -191,17 +191,6 @@ int tm_batch_set_launch(tm_batch* b, int rows_per_task, int ctas_per_sm);
 int tm_batch_get_launch(const tm_batch* b, int* rows_per_task, int* ctas_per_sm);
 int tm_batch_autotune(tm_batch* b, int steps_per_trial);
 
-/* Loop form of the Poisson search inside the FP32 draw of the DP step (Euler-exact
- * remainder, exact sampler; other models ignore it).  The two forms produce the
- * same draws bit for bit and differ in speed: form 0 is faster on dense lattices,
- * form 1 late in near-critical runs.  mode 0 (the default) chooses by timing: every
- * 8th replay of a 32-step graph runs the other form, and the batch switches when that
- * replay took under 97 % of the mean of the replays before and after it; an upload
- * restarts at form 0.  mode 1 or 2 fixes form 0 or 1.  tm_batch_get_draw_variant
- * reports the mode and the form in use. */
-int tm_batch_set_draw_variant(tm_batch* b, int mode);
-int tm_batch_get_draw_variant(const tm_batch* b, int* mode, int* form);
-
 /* Spreading runs (DP, stochastic): spreading_exp_Dornic_2D
  * (stochasticSPDP.cpp:1145-1298) started from a single seed.  With enable = 1,
  * every measurement also gives f2 = the sum over occupied sites (rho > 0) of the

@@ -142,37 +142,6 @@ def test_launch_shape_and_path_invariance(tmg, ctx, precision):
         assert np.array_equal(r, res[0])
 
 
-def test_search_forms_give_the_same_draws(tmg, oracle, ctx):
-    """Both loop forms of the FP32 Poisson search, fixed or chosen by timing during the
-    run (20 graph replays: the automatic mode runs the other form twice), leave the same
-    fields bit for bit, and the oracle's."""
-    model = tmg.dp_model()
-    Ls = [64, 128, 96]
-    seeds = [5, 6, 7]
-    inst = tmg.instances(Ls, seeds, 0.53)
-    init = [f.astype(np.float32) for f in _init_fields(Ls, 3)]
-    n = 32 * 20 + 5
-    res = []
-    for mode in (1, 2, 0):
-        b = tmg.Batch(ctx, model, inst, tmg.TM_FP32)
-        b.set_draw_variant(mode)
-        b.upload(init)
-        b.advance(n)
-        got_mode, form = b.get_draw_variant()
-        assert got_mode == mode and form in (0, 1)
-        if mode:
-            assert form == mode - 1
-        res.append(b.download_packed())
-        b.close()
-    assert np.array_equal(res[0], res[1]) and np.array_equal(res[0], res[2])
-    _, _, ofin, _ = oracle.dp_run(_oracle_dp_params(oracle, model, 0.53, 0.0), init[0], seeds[0], n, [n])
-    assert np.array_equal(tmg.unpack(res[2], inst, 1)[0], ofin)
-    b = tmg.Batch(ctx, model, inst, tmg.TM_FP32)
-    with pytest.raises(RuntimeError):
-        b.set_draw_variant(3)
-    b.close()
-
-
 def test_upload_paths_agree(tmg, ctx):
     """Uploads from pageable memory (copy engines), from page-locked memory (copy kernel)
     and from page-locked memory 4 bytes off a 16-byte boundary (copy engines) leave the

@@ -111,8 +111,6 @@ def test_invalid_arguments_are_rejected_without_gpu(tmlib):
         "tm_mlp_predict": (None, None, 0, None),
         "tm_set_test_probe": (None, 0),
         "tm_batch_set_spreading": (None, 1, -1, -1),
-        "tm_batch_set_draw_variant": (None, 0),
-        "tm_batch_get_draw_variant": (None, None, None),
         "tm_fke_advdiff_device_ws": (None, None, None, None, 1, 0, 1.0, 1e-10, None, 1, None, 1, None, None, 0,
                                      None),
     }

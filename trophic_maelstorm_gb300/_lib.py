@@ -34,7 +34,6 @@ EXPORTS = (
     "tm_mlp_create", "tm_mlp_destroy", "tm_mlp_set_params", "tm_mlp_get_params", "tm_mlp_set_data",
     "tm_mlp_loss_grad", "tm_mlp_train", "tm_mlp_predict", "tm_set_test_probe",
     "tm_fke_workspace_bytes", "tm_fke_advdiff_device_ws", "tm_batch_set_spreading",
-    "tm_batch_set_draw_variant", "tm_batch_get_draw_variant",
 )
 
 
@@ -101,8 +100,6 @@ def lib():
             "tm_batch_enqueue_steps": ([vp, i64], C.c_int),
             "tm_batch_set_launch": ([vp, C.c_int, C.c_int], C.c_int),
             "tm_batch_get_launch": ([vp, C.POINTER(C.c_int), C.POINTER(C.c_int)], C.c_int),
-            "tm_batch_set_draw_variant": ([vp, C.c_int], C.c_int),
-            "tm_batch_get_draw_variant": ([vp, C.POINTER(C.c_int), C.POINTER(C.c_int)], C.c_int),
             "tm_batch_autotune": ([vp, C.c_int], C.c_int),
             "tm_run_dp": ([vp, C.POINTER(DPModel), C.POINTER(Instance), C.c_int, C.c_int, vp, i64, i64p, C.c_int,
                            dp, u32p, vp], C.c_int),

@@ -250,18 +250,6 @@ class Batch:
         T.check(T.lib().tm_batch_get_launch(self._h, C.byref(r), C.byref(c)), "tm_batch_get_launch")
         return r.value, c.value
 
-    def set_draw_variant(self, mode=0):
-        """Loop form of the Poisson search in the FP32 DP draw: 0 chooses by timing
-        (default), 1 and 2 fix form 0 or 1.  The forms give the same draws bit for
-        bit (tm_batch_set_draw_variant)."""
-        T.check(T.lib().tm_batch_set_draw_variant(self._h, int(mode)), "tm_batch_set_draw_variant")
-
-    def get_draw_variant(self):
-        """(mode, form in use)."""
-        m, f = C.c_int(), C.c_int()
-        T.check(T.lib().tm_batch_get_draw_variant(self._h, C.byref(m), C.byref(f)), "tm_batch_get_draw_variant")
-        return m.value, f.value
-
     def autotune(self, steps_per_trial=4):
         T.check(T.lib().tm_batch_autotune(self._h, steps_per_trial), "tm_batch_autotune")
         return self.get_launch()

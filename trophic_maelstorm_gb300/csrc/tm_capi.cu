@@ -99,21 +99,7 @@ struct tm_batch {
     double* d_obs = nullptr;
     int obs_cap = 0;
 
-    cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};   // [search form][parity]
-
-    // Form of the FP32 straight-line draw's Poisson search (tm_batch_set_draw_variant):
-    // both give the same draws; which is faster depends on the lattice's density.
-    // In the automatic mode three consecutive graph replays of every kAbPeriod are
-    // timed, the middle one running the other form, and the batch switches when that
-    // replay beats the mean of its two neighbours.
-    int draw_mode = 0;          // 0 automatic, 1 form 0, 2 form 1
-    int draw_cur = 0;           // form used now
-    long long n_replays = 0;    // graph replays queued in the automatic mode
-    struct AbSlot {
-        cudaEvent_t e0 = nullptr, e1 = nullptr;
-        long long replay = -1;  // replay timed in this slot, -1 when empty
-        int form = 0;
-    } ab[3];
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
 
     InstTables tables() const
     {
@@ -130,19 +116,10 @@ int obs_w(const tm_batch* b) { return b->model == 0 ? (b->spreading ? 3 : 2) : 4
 
 void free_graphs(tm_batch* b)
 {
-    for (auto& row : b->graph)
-        for (auto& g : row) {
-            if (g) cudaGraphExecDestroy(g);
-            g = nullptr;
-        }
-}
-
-// The search form matters only for the FP32 DP step with the Euler-exact remainder
-// and the exact sampler (the instantiation that has both forms).
-bool draw_forms_apply(const tm_batch* b)
-{
-    return b->precision == TM_FP32 && b->model == 0 && !b->dpm.deterministic &&
-           b->dpm.remainder == TM_REM_EULER_EXACT && b->dpm.sampler == TM_SAMPLER_EXACT;
+    for (auto& g : b->graph) {
+        if (g) cudaGraphExecDestroy(g);
+        g = nullptr;
+    }
 }
 
 // Rows per warp task for a new batch: 8, or fewer when the batch is too small
@@ -221,11 +198,9 @@ int warp_grid(const tm_batch* b, int n_tasks)
 }
 
 template <typename T>
-DornicArgs<T> dornic_args(const tm_batch* b, const T* in, T* out, const long long* step_base, long long step_off,
-                          int form = 0)
+DornicArgs<T> dornic_args(const tm_batch* b, const T* in, T* out, const long long* step_base, long long step_off)
 {
     DornicArgs<T> a{};
-    a.draw_variant = form;
     a.in = in; a.out = out; a.it = b->tables(); a.tasks = b->d_tasks; a.n_tasks = b->n_tasks;
     a.step_base = step_base; a.step_off = step_off; a.rows_cap = b->rows_per_task;
     a.cap1 = (b->probe & TM_PROBE_SAMPLER_CAP1) ? 1 : 0;
@@ -279,7 +254,7 @@ RK4Args<T> rk4_args(const tm_batch* b, const T* in, const T* pstar, T* out)
 
 // Queue one step reading buf[src_idx], writing buf[src_idx ^ 1].
 template <typename T>
-cudaError_t enqueue_step_t(tm_batch* b, int src_idx, const long long* step_base, long long step_off, int form)
+cudaError_t enqueue_step_t(tm_batch* b, int src_idx, const long long* step_base, long long step_off)
 {
     cudaStream_t s = b->ctx->stream;
     const T* in = (const T*)b->buf[src_idx];
@@ -303,7 +278,7 @@ cudaError_t enqueue_step_t(tm_batch* b, int src_idx, const long long* step_base,
                               step_base, step_off, b->d_consts, s);
             if (e != cudaSuccess) return e;
         }
-        DornicArgs<T> a = dornic_args<T>(b, in, out, step_base, step_off, form);
+        DornicArgs<T> a = dornic_args<T>(b, in, out, step_base, step_off);
         e = launch_dornic<T>(a, m.remainder == TM_REM_RK4 ? 1 : 0, warp_grid(b, b->n_tasks), 256, s);
         if (e == cudaSuccess && b->spreading) e = launch_border_stop<T>(out, b->tables(), b->n_inst, s);
         return e;
@@ -321,60 +296,29 @@ cudaError_t enqueue_step_t(tm_batch* b, int src_idx, const long long* step_base,
     return launch_rk4<T>(r, false, grid_rk, s);
 }
 
-cudaError_t enqueue_step(tm_batch* b, int src_idx, const long long* step_base, long long step_off, int form)
+cudaError_t enqueue_step(tm_batch* b, int src_idx, const long long* step_base, long long step_off)
 {
-    return b->precision == TM_FP64 ? enqueue_step_t<double>(b, src_idx, step_base, step_off, form)
-                                   : enqueue_step_t<float>(b, src_idx, step_base, step_off, form);
+    return b->precision == TM_FP64 ? enqueue_step_t<double>(b, src_idx, step_base, step_off)
+                                   : enqueue_step_t<float>(b, src_idx, step_base, step_off);
 }
 
-int ensure_graph(tm_batch* b, int form, int parity)
+int ensure_graph(tm_batch* b, int parity)
 {
-    if (b->graph[form][parity]) return TM_OK;
+    if (b->graph[parity]) return TM_OK;
     cudaStream_t s = b->ctx->stream;
     cudaGraph_t g = nullptr;
     TM_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaSuccess;
-    for (int k = 0; k < kGraphSteps && e == cudaSuccess; ++k)
-        e = enqueue_step(b, (parity + k) & 1, b->d_step, k, form);
+    for (int k = 0; k < kGraphSteps && e == cudaSuccess; ++k) e = enqueue_step(b, (parity + k) & 1, b->d_step, k);
     cudaError_t e2 = cudaStreamEndCapture(s, &g);
     if (e != cudaSuccess || e2 != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
         (void)cudaGetLastError();
         return TM_ERR_CUDA;
     }
-    e = cudaGraphInstantiate(&b->graph[form][parity], g, 0);
+    e = cudaGraphInstantiate(&b->graph[parity], g, 0);
     cudaGraphDestroy(g);
     TM_CUDA(e);
-    return TM_OK;
-}
-
-constexpr int kAbPeriod = 8;         // every 8th replay of the automatic mode runs the other form
-constexpr float kAbMargin = 0.97f;   // ... and the batch switches when it took under 97 % of its neighbours
-
-// The timed trio of the automatic mode: once its three replays have run (waiting for
-// them when `wait`, else only if they have), compare the middle replay, which ran the
-// other form, with the mean of its neighbours, switch forms if it was faster by the
-// margin, and empty the slots.
-int ab_settle(tm_batch* b, bool wait)
-{
-    for (auto& sl : b->ab) {
-        if (sl.replay < 0) return TM_OK;   // trio not complete
-        if (wait) {
-            TM_CUDA(cudaEventSynchronize(sl.e1));
-        } else if (cudaEventQuery(sl.e1) != cudaSuccess) {
-            (void)cudaGetLastError();      // still queued (cudaErrorNotReady)
-            return TM_OK;
-        }
-    }
-    float ms[3];
-    bool ok = true;
-    for (int i = 0; i < 3; ++i) ok = ok && cudaEventElapsedTime(&ms[i], b->ab[i].e0, b->ab[i].e1) == cudaSuccess;
-    (void)cudaGetLastError();
-    const tm_batch::AbSlot* t = b->ab;
-    if (ok && t[1].replay == t[0].replay + 1 && t[2].replay == t[1].replay + 1 && t[0].form == b->draw_cur &&
-        t[2].form == b->draw_cur && t[1].form != b->draw_cur && ms[1] < kAbMargin * 0.5f * (ms[0] + ms[2]))
-        b->draw_cur = t[1].form;
-    for (auto& sl : b->ab) sl.replay = -1;
     return TM_OK;
 }
 
@@ -382,46 +326,17 @@ int ab_settle(tm_batch* b, bool wait)
 int run_steps(tm_batch* b, int64_t n)
 {
     cudaStream_t s = b->ctx->stream;
-    const bool forms = draw_forms_apply(b);
-    if (!forms) b->draw_cur = 0;
-    else if (b->draw_mode != 0) b->draw_cur = b->draw_mode - 1;
     while (n > 0) {
         if (n >= kGraphSteps) {
-            // automatic mode: time the replays around and at every kAbPeriod-th one,
-            // which runs the other form (not while the stream is being captured)
-            cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-            tm_batch::AbSlot* sl = nullptr;
-            int form = b->draw_cur;
-            if (forms && b->draw_mode == 0 && cudaStreamIsCapturing(s, &cap) == cudaSuccess &&
-                cap == cudaStreamCaptureStatusNone) {
-                const long long r = b->n_replays++;
-                const int k = (int)(r % kAbPeriod) - (kAbPeriod / 2 - 1);   // 0, 1, 2: the timed trio
-                // the previous trio: settled when it has run; at the start of a new trio
-                // the host waits for it (it is kAbPeriod - 3 replays back, so the device
-                // still has queued work)
-                int rc = ab_settle(b, k == 0);
-                if (rc != TM_OK) return rc;
-                if (k == 1) form = 1 - b->draw_cur;
-                if (k >= 0 && k <= 2) {
-                    sl = &b->ab[k];
-                    if (!sl->e0) TM_CUDA(cudaEventCreate(&sl->e0));
-                    if (!sl->e1) TM_CUDA(cudaEventCreate(&sl->e1));
-                    sl->replay = r;
-                    sl->form = form;
-                }
-            }
-            // the graph is built before the first event, so a replay's time holds no build
-            int rc = ensure_graph(b, form, b->cur);
+            int rc = ensure_graph(b, b->cur);
             if (rc != TM_OK) return rc;
-            if (sl) TM_CUDA(cudaEventRecord(sl->e0, s));
             TM_CUDA(launch_set_step(b->d_step, b->step, s));
-            TM_CUDA(cudaGraphLaunch(b->graph[form][b->cur], s));
-            if (sl) TM_CUDA(cudaEventRecord(sl->e1, s));
+            TM_CUDA(cudaGraphLaunch(b->graph[b->cur], s));
             b->step += kGraphSteps;
             n -= kGraphSteps;
             // kGraphSteps is even: the current buffer is unchanged
         } else {
-            TM_CUDA(enqueue_step(b, b->cur, nullptr, b->step, b->draw_cur));
+            TM_CUDA(enqueue_step(b, b->cur, nullptr, b->step));
             b->cur ^= 1;
             b->step += 1;
             n -= 1;
@@ -595,10 +510,6 @@ int tm_batch_destroy(tm_batch* b)
     cudaSetDevice(b->ctx->device);
     cudaStreamSynchronize(b->ctx->stream);
     free_graphs(b);
-    for (auto& sl : b->ab) {
-        if (sl.e0) cudaEventDestroy(sl.e0);
-        if (sl.e1) cudaEventDestroy(sl.e1);
-    }
     cudaFree(b->buf[0]); cudaFree(b->buf[1]); cudaFree(b->aux); cudaFree(b->site_b);
     cudaFree(b->d_dlist); cudaFree(b->d_dcnt);
     cudaFree(b->d_step); cudaFree(b->d_off); cudaFree(b->d_fstride); cudaFree(b->d_L); cudaFree(b->d_seed);
@@ -704,10 +615,6 @@ int64_t tm_batch_step(const tm_batch* b) { return b ? b->step : -1; }
 static int reset_after_upload(tm_batch* b, int64_t step)
 {
     b->step = step;
-    // a new state: the search form restarts at form 0 (automatic mode) with no timings
-    b->draw_cur = b->draw_mode ? b->draw_mode - 1 : 0;
-    b->n_replays = 0;
-    for (auto& sl : b->ab) sl.replay = -1;
     cudaStream_t s = b->ctx->stream;
     std::vector<int> ones(b->n_inst, 1);
     TM_CUDA(cudaMemcpyAsync(b->d_alive, ones.data(), b->n_inst * sizeof(int), cudaMemcpyHostToDevice, s));
@@ -871,24 +778,6 @@ int tm_batch_set_launch(tm_batch* b, int rows, int ctas)
     if (rows > 0 && rows != b->rows_per_task) { b->rows_per_task = rows; rebuild = true; }
     if (ctas > 0 && ctas != b->ctas_per_sm) { b->ctas_per_sm = ctas; free_graphs(b); }
     return rebuild ? build_tasks(b) : TM_OK;
-}
-
-int tm_batch_set_draw_variant(tm_batch* b, int mode)
-{
-    if (!b || mode < 0 || mode > 2) return TM_ERR_INVALID;
-    b->draw_mode = mode;
-    b->draw_cur = mode ? mode - 1 : 0;
-    b->n_replays = 0;
-    for (auto& sl : b->ab) sl.replay = -1;
-    return TM_OK;
-}
-
-int tm_batch_get_draw_variant(const tm_batch* b, int* mode, int* form)
-{
-    if (!b) return TM_ERR_INVALID;
-    if (mode) *mode = b->draw_mode;
-    if (form) *form = draw_forms_apply(b) ? b->draw_cur : 0;
-    return TM_OK;
 }
 
 int tm_batch_get_launch(const tm_batch* b, int* rows, int* ctas)

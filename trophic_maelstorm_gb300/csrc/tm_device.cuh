@@ -574,11 +574,6 @@ __device__ __forceinline__ T dornic_draw(Stream<T>& g, T m, T mu1, T inv_lambda,
 constexpr int kFastInv = 32;
 static_assert(kFastInv % 4 == 0, "the inversion takes four terms per trip");
 
-// INV selects the form of the Poisson search's loop (INV = 0: a test after the second
-// and the fourth term of each trip; INV = 1: one test per trip, the last trip's count
-// from its first three differences).  Both give the same count, so the same draw;
-// they differ in speed by regime (dense lattices favour 0, dilute ones 1).
-template <int INV = 0>
 __device__ __forceinline__ float dornic_draw_fast(uint64_t seed, uint32_t site, int64_t step, float m, float mu1,
                                                   float inv_lambda, int sampler, const SmemTab<float>& tb,
                                                   bool& deferred)
@@ -616,52 +611,27 @@ __device__ __forceinline__ float dornic_draw_fast(uint64_t seed, uint32_t site, 
         float q = small ? tm_negexpm1(m) : 1.0f - p;
         if (small && u < q) p = tm_exp_neg_small(-m);
         // four terms per trip: the same products and differences as one term
-        // per trip (kFastInv is a multiple of 4).  q only decreases (p >= 0), so
-        // the terms with u < q form a prefix of the search and a test after term j
-        // tells whether the search ends by then; the terms before it that still had
-        // u < q complete the count -- the count a test after every term gives.
+        // per trip (kFastInv is a multiple of 4), tested after the second and
+        // the fourth term.  q only decreases (p >= 0), so the terms with u < q
+        // form a prefix, and a failed test counts the one term before it that
+        // still had u < q -- the same count as testing every term, with half the
+        // branches.
         int it = 0;
-        if constexpr (INV == 0) {
-            // tests after the second and the fourth term
-            while (u < q && it < kFastInv) {
-                const float4 r4 = *reinterpret_cast<const float4*>(tb.rcp + it + 1);
-                const float p1 = (p * m) * r4.x;
-                const float q1 = q - p1;
-                const float p2 = (p1 * m) * r4.y;
-                const float q2 = q1 - p2;
-                if (!(u < q2)) { it += 1 + (int)(u < q1); q = q2; break; }
-                const float p3 = (p2 * m) * r4.z;
-                const float q3 = q2 - p3;
-                p = (p3 * m) * r4.w;
-                q = q3 - p;
-                if (!(u < q)) { it += 3 + (int)(u < q3); break; }
-                it += 4;
-            }
-            if (u < q) { deferred = true; return 0.0f; }
-        } else {
-            // one test per trip
-            bool go = u < q;
-            while (go) {
-                const float4 r4 = *reinterpret_cast<const float4*>(tb.rcp + it + 1);
-                const float p1 = (p * m) * r4.x;
-                const float q1 = q - p1;
-                const float p2 = (p1 * m) * r4.y;
-                const float q2 = q1 - p2;
-                const float p3 = (p2 * m) * r4.z;
-                const float q3 = q2 - p3;
-                const float p4 = (p3 * m) * r4.w;
-                const float q4 = q3 - p4;
-                if (u < q4) {
-                    if (it + 4 >= kFastInv) { deferred = true; return 0.0f; }
-                    p = p4;
-                    q = q4;
-                    it += 4;
-                } else {
-                    it += 1 + (int)(u < q1) + (int)(u < q2) + (int)(u < q3);
-                    go = false;
-                }
-            }
+        while (u < q && it < kFastInv) {
+            const float4 r4 = *reinterpret_cast<const float4*>(tb.rcp + it + 1);
+            const float p1 = (p * m) * r4.x;
+            const float q1 = q - p1;
+            const float p2 = (p1 * m) * r4.y;
+            const float q2 = q1 - p2;
+            if (!(u < q2)) { it += 1 + (int)(u < q1); q = q2; break; }
+            const float p3 = (p2 * m) * r4.z;
+            const float q3 = q2 - p3;
+            p = (p3 * m) * r4.w;
+            q = q3 - p;
+            if (!(u < q)) { it += 3 + (int)(u < q3); break; }
+            it += 4;
         }
+        if (u < q) { deferred = true; return 0.0f; }
         n = (float)it;
     }
     const float k = mu1 + n;

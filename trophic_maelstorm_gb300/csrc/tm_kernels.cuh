@@ -54,7 +54,6 @@ struct DornicArgs {
     long long seg_cap;             // entries per segment (all sites of one warp's tasks)
     long long dlist_cap;           // entries the list holds
     long long max_seg;             // segments dcnt holds
-    int draw_variant;              // FP32 DP, exact sampler: form of the Poisson search (0 or 1, same draws)
 };
 
 template <typename T>

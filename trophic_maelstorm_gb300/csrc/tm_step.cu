@@ -106,9 +106,8 @@ __device__ __forceinline__ void draw_general_site(const DornicArgs<T>& A, const 
 // code, which keeps the loop body small for the instruction cache.  CAP is the
 // attempts of each rejection loop: kSamplerCap, or 1 in the instantiation that
 // TM_PROBE_SAMPLER_CAP1 selects (the straight-line draw makes one attempt of
-// each loop, so it is unchanged).  INV is the form of the straight-line draw's
-// Poisson search (dornic_draw_fast): the same draws, a different speed by regime.
-template <typename T, int REM, int SAMP, int CAP, int INV = 0>
+// each loop, so it is unchanged).
+template <typename T, int REM, int SAMP, int CAP>
 __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_kernel(const DornicArgs<T> A)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -235,8 +234,8 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 ? 4 : 2)) dornic_step_ker
                     if (has) {
                         const int li = Wqi[j];
                         const uint32_t site = site_index(y0 + (li >> 5), L, x0 + (li & 31));
-                        const float v = dornic_draw_fast<INV>(seed, site, step, Wqm[j], Wqmu[j],
-                                                              inv_lambda, SAMP, tab, deferred);
+                        const float v = dornic_draw_fast(seed, site, step, Wqm[j], Wqmu[j], inv_lambda, SAMP, tab,
+                                                         deferred);
                         if constexpr (kStoreEarly) {
                             if (!deferred) {
                                 const long long o = (long long)(y0 + (li >> 5)) * L + x0 + (li & 31);
@@ -360,13 +359,13 @@ __global__ void __launch_bounds__(256) dornic_deferred_kernel(const DornicArgs<T
     }
 }
 
-template <typename T, int REM, int SAMP, int CAP = kSamplerCap, int INV = 0>
+template <typename T, int REM, int SAMP, int CAP = kSamplerCap>
 cudaError_t launch_dornic_t(const DornicArgs<T>& a, int grid, int block, size_t smem, cudaStream_t s)
 {
     static bool attr_set = false;
     if (!attr_set) {
         const int full = (int)(warp_scratch_bytes<T>(kMaxRowsPerTask) * kWarps);
-        const cudaError_t e = cudaFuncSetAttribute(dornic_step_kernel<T, REM, SAMP, CAP, INV>,
+        const cudaError_t e = cudaFuncSetAttribute(dornic_step_kernel<T, REM, SAMP, CAP>,
                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, full);
         if (e != cudaSuccess) return e;
         attr_set = true;
@@ -379,7 +378,7 @@ cudaError_t launch_dornic_t(const DornicArgs<T>& a, int grid, int block, size_t 
             (long long)n_seg * a.seg_cap > a.dlist_cap)
             return cudaErrorInvalidValue;
     }
-    dornic_step_kernel<T, REM, SAMP, CAP, INV><<<grid, block, smem, s>>>(a);
+    dornic_step_kernel<T, REM, SAMP, CAP><<<grid, block, smem, s>>>(a);
     if constexpr (sizeof(T) == 4) dornic_deferred_kernel<T, REM, SAMP, CAP><<<(n_seg + 7) / 8, 256, 0, s>>>(a, n_seg);
     return cudaGetLastError();
 }
@@ -390,11 +389,6 @@ cudaError_t launch_dornic_r(const DornicArgs<T>& a, int grid, int block, size_t 
     if (a.cap1) {  // the sampler-cap probe: DP, Euler-exact remainder, exact sampler only
         if (REM == 0 && a.sampler == 0) return launch_dornic_t<T, 0, 0, 1>(a, grid, block, smem, s);
         return cudaErrorInvalidValue;
-    }
-    if constexpr (sizeof(T) == 4 && REM == 0) {
-        // the second form of the Poisson search, for the DP step with the exact sampler
-        if (a.sampler == 0 && a.draw_variant == 1)
-            return launch_dornic_t<T, 0, 0, kSamplerCap, 1>(a, grid, block, smem, s);
     }
     if (a.sampler == 0) return launch_dornic_t<T, REM, 0>(a, grid, block, smem, s);
     if (a.sampler == 1) return launch_dornic_t<T, REM, 1>(a, grid, block, smem, s);
