@@ -11,9 +11,12 @@
 // a straight-line path first; the few sites it defers (a few % of live sites)
 // go to the warp's own segment of a batch-wide list (no atomics: the warp keeps
 // the count) that a second kernel draws with the general sampler, so the step
-// kernel's loop body holds no general-sampler code.  FP64 draws every
-// live site with the general sampler, carried from task to task and drawn 32 at
-// a time.  Per site it fuses:
+// kernel's loop body holds no general-sampler code.  The FP32 DP step stores
+// each site as soon as its value is known: absorbing sites while the rows
+// stream in (pass 1), drawn sites right after their draw (pass 2).  The
+// Rietkerk draw and FP64 keep a third pass that stores from shared memory.  FP64
+// draws every live site with the general sampler, carried from task to task and
+// drawn 32 at a time.  Per site it fuses:
 //   alpha_i  = (D/dx^2) * sum of the 4 neighbours       stochasticSPDP.cpp:1037-1038
 //   skip     if alpha_i == 0 and rho_i == 0             :1049-1052
 //   rho*     = Gamma(2 alpha_i/sigma^2 + Poisson(lambda e^{beta dt} rho_i)) / lambda   :1053-1059
