@@ -138,15 +138,17 @@ def test_spectrum_restatement_matches_reference_estimator():
         np.testing.assert_allclose(p, want, rtol=1e-12, atol=1e-12 * max(1.0, want.max()))
 
 
-def test_rietkerk_ensemble_matches_reference(oracle, golden):
-    """The oracle's stochastic Rietkerk step (Philox, own samplers) against replicates of
-    the reference's step (its P-Dornic loop with libstdc++ draws, its compiled remainder RK4,
-    the clamp): 400 replicates of 500 steps on a 16^2 start with bare and nearly bare
-    patches; final mean P, W, O, occupied sites and two single-site values."""
+@pytest.mark.parametrize("dtype", [np.float64, np.float32], ids=["fp64", "fp32"])
+def test_rietkerk_ensemble_matches_reference(oracle, golden, dtype):
+    """The oracle's stochastic Rietkerk step (Philox, own samplers), FP64 and FP32 state,
+    against replicates of the reference's step (its P-Dornic loop with libstdc++ draws, its
+    compiled remainder RK4, the clamp): 400 replicates of 500 steps on a 16^2 start with bare
+    and nearly bare patches; final mean P, W, O, occupied sites and two single-site values."""
     from conftest import rk_ensemble_rows, assert_same_ensemble
     g = golden["rk_ens"]
     L, R, sigma, dt, steps, n_rep, _, eps = g["meta"]
     steps, n_rep = int(steps), int(n_rep)
     p = oracle.rk_params(R=R, sigma=sigma, dt=dt, clamp_eps=eps)
-    fins = [oracle.rk_run(p, g["start"], j, steps, [steps])[2] for j in range(n_rep)]
+    start = g["start"].astype(dtype)
+    fins = [oracle.rk_run(p, start, j, steps, [steps])[2] for j in range(n_rep)]
     assert_same_ensemble(rk_ensemble_rows(fins), g["rows"], g["columns"])
